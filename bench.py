@@ -1,0 +1,377 @@
+"""Benchmark: batched validate_motion on the 65,536-edge Panda workload, edges validated per second.
+
+Workload (one step): 65,536 straight-line Panda edges with endpoints uniform within the joint
+limits, checked at the robot's resolution (32) against a seeded scene of 24 spheres, 24 cuboids
+and 12 capsules in the 4 m workspace volume (about 45% of edges collide).  Inputs are synthetic
+(seeded) stand-ins for the reference's MotionBenchMaker problems.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+GPU arm: `value` times the persistent edge kernel alone with CUDA events on its stream, inputs
+resident in HBM, the L2 flushed (256 MB write) between timed steps.  `e2e` times the C-ABI
+call with host buffers (pinned), copies in and out included.  `roofline` relates the kernel's
+algorithmic FP32 work (counted by the CPU oracle on a sample of the same edges) to the FP32 peak.
+Reference arm: the reference's CPU algorithm on the host cores (the compiled reference where it
+runs, else the CPU oracle that restates it).  N > 1 runs independent replicas, one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_EDGES = 65536
+RESOLUTION = 32
+SCENE_SEED = 1
+EDGE_SEED = 2024
+METRIC = "edges validated/s on 1 GB300, learned-order vs plain GPU path, identical verdicts"
+WORKLOAD = "panda validate_motion batch: 65536 edges, res 32, 24 spheres + 24 cuboids + 12 capsules"
+
+# FP32 work per primitive test / query, in floating-point operations (fused multiply-add = 2),
+# as the kernels evaluate them (vamp_gb300/csrc/vg_check.cuh)
+FLOPS = {
+    "test": [11, 26, 16, 27, 18],  # sphere, capsule, z-capsule, cuboid, z-cuboid
+    "break_check": 1,  # min_distance - max_extent, per object visited
+    "query": 8,  # |c|^2, max_extent, r^2 per sphere query
+    "self_pair": 11,
+}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if _has_cuda() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def _has_cuda():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _has_cuda() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload():
+    from vamp_gb300 import scenes
+    from vamp_gb300.robots import model
+
+    m = model("panda")
+    s_m = np.array(m["s_m"], np.float32)
+    s_a = np.array(m["s_a"], np.float32)
+    scene = scenes.scene_config1(SCENE_SEED)
+    a, b = scenes.edges(s_m, s_a, N_EDGES, EDGE_SEED)
+    return scene, a, b
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_flops(scene, a, b, sample: int = 8192):
+    """FP32 operations the reference's algorithm performs on the workload, from the CPU oracle's
+    work counters on a sample of the edges (scaled to the full batch)."""
+    from oracle.vgo import Port
+    from vamp_gb300.robotgen.codegen import fk_flops
+    from vamp_gb300.robots import model
+
+    port = Port()
+    rb = port.robot("panda")
+    env = port.env(scene)
+    _, cnt = env.validate_motions_counted(rb, a[:sample], b[:sample], RESOLUTION)
+    fk = fk_flops(model("panda"))
+    lanes = cnt.lanes
+    tests = sum(int(cnt.tests[k]) * FLOPS["test"][k] for k in range(5))
+    per_lane_fk = fk["frames"] + fk["centre"] * fk["slots"]
+    flops = (lanes * per_lane_fk + tests + sum(int(cnt.tests[k]) for k in range(5)) * FLOPS["break_check"]
+             + int(cnt.sphere_queries) * FLOPS["query"] + int(cnt.self_pairs) * FLOPS["self_pair"])
+    scale = len(a) / sample
+    return {"flops": flops * scale, "blocks": int(cnt.blocks) * scale, "lanes": lanes * scale,
+            "tests": sum(int(t) for t in cnt.tests) * scale, "per_lane_fk": per_lane_fk}
+
+
+def fp32_peak_tflops(device_props, sm_mhz: float | None):
+    """FP32 (non-tensor) peak: 128 FP32 lanes x 2 FLOP per SM per clock."""
+    sms = device_props.multi_processor_count
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    mhz = peaks.get("sm_max_mhz", 2070.0)
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, mhz, sms
+
+
+def cpu_baseline(scene, a, b, budget_s: float = 10.0):
+    """The reference's algorithm on the host cores: the compiled reference when it loads here,
+    else the CPU oracle.  Bounded sample: whole passes over a slice of the edges until about
+    `budget_s` seconds have been spent."""
+    threads = os.cpu_count() or 1
+    kind = "port"
+    fn = None
+    try:
+        from oracle.vgo import REF_LIB, Reference
+
+        if REF_LIB.exists():
+            ref = Reference()
+            renv = ref.env(scene)
+            fn = lambda x, y: renv.validate_motions("panda", x, y, RESOLUTION, threads=threads)  # noqa: E731
+            kind = "reference"
+    except Exception:
+        fn = None
+    if fn is None:
+        from oracle.vgo import Port
+
+        port = Port()
+        penv = port.env(scene)
+        rb = port.robot("panda")
+        fn = lambda x, y: penv.validate_motions(rb, x, y, RESOLUTION, threads=threads)[0]  # noqa: E731
+        kind = "port"
+    n = min(len(a), 4096)
+    t0 = time.perf_counter()
+    fn(a[:n], b[:n])
+    dt = time.perf_counter() - t0
+    rate = n / max(dt, 1e-9)
+    n = int(min(len(a), max(4096, rate * budget_s)))
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s * 0.5 or done == 0:
+        fn(a[:n], b[:n])
+        done += n
+    elapsed = time.perf_counter() - t0
+    return {"value": done / elapsed, "unit": "edges/s", "cores": threads, "kind": kind,
+            "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    scene, a, b = workload()
+    times = []
+    res = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(scene, a, b, budget_s=4.0)
+        if i >= args.warmup:
+            times.append(1.0 / r["value"])
+            res = r
+    value = 1.0 / float(np.mean(times))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "edges/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * N_EDGES / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene and edges)",
+        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "l2": "host CPU run"},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": res["cores"], "kind": res["kind"], "sample": res["sample"]},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300._lib import check, lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    scene, a_np, b_np = workload()
+    env = vg.Environment.from_scene(scene)
+    a = torch.from_numpy(a_np).to(dev)
+    b = torch.from_numpy(b_np).to(dev)
+    out = torch.empty(N_EDGES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def launch():
+        check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
+                                             out.data_ptr(), None, stream.cuda_stream))
+
+    for _ in range(max(args.warmup, 3)):
+        launch()
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.zero_()  # evict the inputs from L2 between timed steps
+            starts[i].record(stream)
+            launch()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kernel_ms = float(np.mean(step_ms))
+    kernel_ms = max_over_ranks(world, kernel_ms)
+    value = world * N_EDGES / (kernel_ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    pa = torch.empty(a_np.shape, dtype=torch.float32, pin_memory=True).numpy()
+    pb = torch.empty(b_np.shape, dtype=torch.float32, pin_memory=True).numpy()
+    pa[:] = a_np
+    pb[:] = b_np
+    pout = np.zeros(N_EDGES, np.uint8)
+    for _ in range(max(args.warmup, 3)):
+        vg.panda.validate_motion_batch(pa, pb, env, RESOLUTION, out=pout)
+    barrier(world)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vg.panda.validate_motion_batch(pa, pb, env, RESOLUTION, out=pout)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(world, float(np.mean(e2e_t)))
+    gpu_verdicts = out.cpu().numpy()
+    assert np.array_equal(gpu_verdicts, pout), "device and host-buffer calls disagree"
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "edges/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": kernel_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene and edges)",
+        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "order": "plain (reference block order)",
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "colliding_fraction": float(1 - gpu_verdicts.mean())},
+        "gpu_launches": args.steps,
+        "e2e": {"value": world * N_EDGES / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": int(a_np.nbytes + b_np.nbytes),
+                "d2h_bytes_per_step": int(N_EDGES)},
+    }
+    clk = clocks.summary()
+    line["clocks"] = clk
+    work = algorithmic_flops(scene, a_np, b_np)
+    peak, mhz, sms = fp32_peak_tflops(torch.cuda.get_device_properties(dev), clk["sm_mhz"] if clk else None)
+    achieved = work["flops"] / (kernel_ms / 1e3) / 1e12
+    line["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "traffic": None,
+                        "note": f"FP32 peak = {sms} SMs x 256 FLOP/clk x {mhz:.0f} MHz (max SM clock of MEASURED_PEAKS.json); "
+                                f"algorithmic FLOPs counted by the CPU oracle on 8192 of the edges, scaled"}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(scene, a_np, b_np)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

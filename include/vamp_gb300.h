@@ -1,0 +1,120 @@
+/* vamp_gb300: GPU (sm_103a) collision checking behind a plain C ABI.
+ *
+ * This is the drop-in boundary for VAMP's data-parallel hot path: batched robot forward
+ * kinematics fused with sphere-vs-environment collision checking.  Every entry point takes
+ * plain pointers and sizes; none allocates on behalf of the caller except where stated.
+ * All functions return VG_OK (0) or a negative VG_ERR_* code; vg_last_error() describes the
+ * last failure of the calling thread.  There is no CPU fallback: without a usable GPU the
+ * check functions fail with VG_ERR_CUDA.
+ *
+ * Semantics.  Verdicts follow the reference's compiled code: an edge is checked in blocks of
+ * `lanes` states exactly as planning::validate_motion<Robot, lanes, resolution> visits them, and
+ * decisions the reference takes per SIMD block (coarse-sphere gating, the early exit of the
+ * primitive loop) are taken per block here too.  vg_env_set_mode() selects which reference
+ * build is reproduced: lanes 8 with the x86 rsqrt-based bound (AVX2, the default) or lanes 4
+ * with an exact square root (NEON).
+ *
+ * Threading.  Calls that share a vg_env must not overlap (they share its scratch counter and
+ * staging buffers); use one environment per concurrent stream.  Environments are not
+ * thread-safe without external locking, like the reference's (planning is single-threaded).
+ *
+ * Reference paths below are relative to the reference's src/impl/vamp/ unless noted.
+ */
+#ifndef VAMP_GB300_H
+#define VAMP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VG_OK 0
+#define VG_ERR_ARG (-1)     /* invalid argument (null pointer, bad size, unknown robot) */
+#define VG_ERR_CUDA (-2)    /* CUDA runtime failure or no usable device */
+#define VG_ERR_NOMEM (-3)   /* host or device allocation failed */
+#define VG_ERR_STATE (-4)   /* operation not valid in the object's current state */
+#define VG_ERR_LIMIT (-5)   /* input exceeds a documented size limit */
+
+#define VG_SQRT_X86 0   /* sqrt(v) = v * rsqrt(v) as the AVX2 build computes it (vector/avx.hh:412-415) */
+#define VG_SQRT_EXACT 1 /* correctly rounded sqrt as the NEON build computes it (vector/neon.hh:520-523) */
+
+typedef struct vg_env vg_env;
+
+/* Message for the calling thread's last error ("" if none). */
+const char *vg_last_error(void);
+const char *vg_version(void);
+
+/* ------------------------------------------------------------------------------- robots
+ * Robots: "panda", "ur5", "fetch", "baxter".  Replaces the per-robot constants of
+ * robots/<robot>.hh:11-18 (dimension, n_spheres, min_radius, max_radius, resolution). */
+int vg_robot_info(const char *robot, int *dim, int *n_spheres, float *r_min, float *r_max, int *resolution);
+/* Joint scaling q = u * s_m + s_a (robots/panda.hh:50-80, scale_configuration).  dim floats each. */
+int vg_robot_limits(const char *robot, float *s_m, float *s_a);
+
+/* --------------------------------------------------------------------------- environment
+ * Replaces collision::Environment<float> and its Python constructors
+ * (collision/environment.hh:15-85, bindings/environment.cc:109-165). */
+vg_env *vg_env_create(void);
+void vg_env_destroy(vg_env *env);
+/* Sphere x y z r (collision/shapes.hh:217-251). */
+int vg_env_add_sphere(vg_env *env, const float *xyzr);
+/* Capsule x1 y1 z1 xv yv zv r rdv with rdv = 1 / (v . v) (collision/shapes.hh:122-214);
+ * stored as z-aligned when xv == yv == 0, as Environment.add_capsule does
+ * (bindings/environment.cc:132-145). */
+int vg_env_add_capsule(vg_env *env, const float *fields8);
+/* Cuboid: centre xyz, axis_1 xyz, axis_2 xyz, axis_3 xyz, half extents (collision/shapes.hh:29-120);
+ * stored as z-aligned when axis_3_z == 1 (bindings/environment.cc:118-131). */
+int vg_env_add_cuboid(vg_env *env, const float *fields15);
+/* Which reference build to reproduce: lanes 8 + VG_SQRT_X86 (default) or lanes 4 + VG_SQRT_EXACT. */
+int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
+/* Number of objects of a kind (0 spheres, 1 capsules, 2 z-capsules, 3 cuboids, 4 z-cuboids)
+ * and the fields of one, in checking order, followed by its min_distance. */
+int vg_env_count(const vg_env *env, int kind, size_t *count);
+int vg_env_get(const vg_env *env, int kind, size_t index, float *out);
+
+/* ----------------------------------------------------------------------- checks (device)
+ * Inputs and outputs in device memory; asynchronous on `stream` (a cudaStream_t, or NULL for
+ * the default stream).  Configurations are row-major [n][dim] float32. */
+
+/* Per-configuration validity: out[i] = 1 if configuration i is collision free.
+ * Replaces Robot::fkcc on a broadcast block, i.e. the Python binding's validate()
+ * (bindings/robot_helper.hh:256-267; robots/panda.hh:5227 fkcc). */
+int vg_validate_states_device(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out, void *stream);
+
+/* Per-edge validity of the straight-line motions a[i] -> b[i]: out[i] = 1 if valid.
+ * Replaces planning::validate_motion<Robot, lanes, resolution> (planning/validate.hh:24-77).
+ * blocks (optional, may be NULL) receives the number of lane-blocks checked per edge. */
+int vg_validate_motions_device(
+    const char *robot,
+    vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream);
+
+/* Sphere centres and radii of every sphere slot (fine spheres, then each checked link's coarse
+ * sphere), out is [n][slots][4].  Replaces Robot::sphere_fk (robots/panda.hh:117-462). */
+int vg_sphere_fk_device(const char *robot, const float *q, size_t n, float *out, void *stream);
+
+/* ------------------------------------------------------------------------- checks (host)
+ * Same as the device forms with host buffers: copies in, checks, copies out, and waits.
+ * Pinned buffers (vg_host_alloc) make the copies fastest.  Staging memory is owned by env. */
+int vg_validate_states(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out);
+int vg_validate_motions(
+    const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution, uint8_t *out);
+int vg_sphere_fk(const char *robot, const float *q, size_t n, float *out);
+
+/* Page-locked host memory for the host-buffer calls. */
+void *vg_host_alloc(size_t bytes);
+void vg_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VAMP_GB300_H */

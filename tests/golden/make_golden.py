@@ -1,0 +1,132 @@
+"""Generates the golden fixtures in this folder from the reference's own compiled code.
+
+The reference (CoMMALab/vamp) ships no tests and no golden vectors, so the fixtures are produced
+by running the reference itself: its hot-path headers compiled from the reference checkout by
+oracle/ref/Makefile (x86-64, AVX2 build, 8 lanes).  Run in a container that has the checkout:
+
+    python tests/golden/make_golden.py [--reference /path/to/vamp]
+
+Every fixture stores its inputs as well as the reference's outputs, so the tests need neither the
+reference nor a particular random-number generator.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.vgo import Port, Reference, build_reference  # noqa: E402
+from vamp_gb300 import scenes  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+ROBOTS = ("panda", "ur5", "fetch", "baxter")
+
+
+def scene_arrays(scene: dict) -> dict:
+    return {"spheres": scene["spheres"], "capsules": scene["capsules"], "cuboids": scene["cuboids"]}
+
+
+def env_dump(env) -> dict:
+    return {f"kind{k}": env.objects(k) for k in range(5)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None)
+    a = ap.parse_args()
+    if build_reference(a.reference) is None:
+        raise SystemExit("reference checkout not found (or not x86-64): cannot generate golden fixtures")
+    ref = Reference()
+    port = Port()
+
+    # --- forward kinematics: fine sphere centres (Robot::sphere_fk)
+    for r in ROBOTS:
+        rb = port.robot(r)
+        q = scenes.configurations(rb.s_m, rb.s_a, 32, 100 + len(r))
+        sph = np.stack([ref.sphere_fk(r, qi, rb.fine) for qi in q])
+        np.savez_compressed(OUT / f"fk_{r}.npz", q=q, spheres=sph)
+
+    # --- per-configuration verdicts (validate(q): validate_motion(q, q) at resolution 1)
+    cases = [
+        ("states_panda_scene0", "panda", scenes.scene_config0(0), 2048, 11),
+        ("states_panda_scene1", "panda", scenes.scene_config1(1), 2048, 12),
+        ("states_ur5_scene1", "ur5", scenes.scene_config1(2), 1024, 13),
+        ("states_fetch_scene1", "fetch", scenes.scene_config1(3), 1024, 14),
+        ("states_baxter_scene1", "baxter", scenes.scene_config1(4), 1024, 15),
+    ]
+    for name, r, scene, n, seed in cases:
+        rb = port.robot(r)
+        q = scenes.configurations(rb.s_m, rb.s_a, n, seed)
+        renv = ref.env(scene)
+        verdict = renv.validate_states(r, q)
+        np.savez_compressed(OUT / f"{name}.npz", q=q, verdict=verdict, **scene_arrays(scene), **env_dump(renv))
+
+    # --- per-edge verdicts (validate_motion<Robot, 8, resolution>)
+    cases = [
+        ("edges_panda_scene1_res32", "panda", scenes.scene_config1(1), 2048, 21, 32),
+        ("edges_panda_scene0_res1", "panda", scenes.scene_config0(0), 1024, 22, 1),
+        ("edges_panda_scene1_res8", "panda", scenes.scene_config1(5), 1024, 23, 8),
+        ("edges_ur5_scene1_res32", "ur5", scenes.scene_config1(2), 512, 24, 32),
+        ("edges_fetch_scene1_res32", "fetch", scenes.scene_config1(3), 512, 25, 32),
+        ("edges_baxter_scene1_res64", "baxter", scenes.scene_config1(4), 256, 26, 64),
+    ]
+    for name, r, scene, n, seed, res in cases:
+        rb = port.robot(r)
+        ea, eb = scenes.edges(rb.s_m, rb.s_a, n, seed)
+        renv = ref.env(scene)
+        verdict = renv.validate_motions(r, ea, eb, res)
+        np.savez_compressed(OUT / f"{name}.npz", a=ea, b=eb, resolution=res, verdict=verdict, **scene_arrays(scene))
+
+    # --- the exact states validate_motion visits, in order (planning/validate.hh:24-67)
+    rb = port.robot("panda")
+    ea, eb = scenes.edges(rb.s_m, rb.s_a, 16, 31)
+    counts, blocks = [], []
+    for i in range(len(ea)):
+        n, blk = ref.motion_blocks("panda", ea[i], eb[i], 32, cap=512, dim=7)
+        counts.append(n)
+        blocks.append(blk.transpose(0, 2, 1))  # [block][lane][dim]
+    np.savez_compressed(
+        OUT / "motion_blocks_panda.npz", a=ea, b=eb, counts=np.array(counts), blocks=np.concatenate(blocks)
+    )
+
+    # --- the 8-lane sqrt of the early-exit bound, and the lane sin/cos
+    rng = np.random.default_rng(41)
+    v = np.concatenate(
+        [rng.uniform(0, 4, 4096), rng.uniform(0, 1e-3, 1024), 10.0 ** rng.uniform(-30, 30, 1024), [0.0] * 8]
+    ).astype(np.float32)
+    v = v[: len(v) // 8 * 8]
+    out = np.zeros_like(v)
+    for i in range(0, len(v), 8):
+        x = np.ascontiguousarray(v[i : i + 8])
+        o = np.zeros(8, np.float32)
+        ref.lib.vgref_vec_sqrt8(x.ctypes.data_as(__import__("ctypes").c_void_p), o.ctypes.data_as(__import__("ctypes").c_void_p))
+        out[i : i + 8] = o
+    ang = rng.uniform(-3.2, 3.9, 4096).astype(np.float32)
+    s = np.zeros_like(ang)
+    c = np.zeros_like(ang)
+    import ctypes
+
+    for i in range(0, len(ang), 8):
+        x = np.ascontiguousarray(ang[i : i + 8])
+        so = np.zeros(8, np.float32)
+        co = np.zeros(8, np.float32)
+        ref.lib.vgref_vec_sincos8(x.ctypes.data_as(ctypes.c_void_p), so.ctypes.data_as(ctypes.c_void_p), co.ctypes.data_as(ctypes.c_void_p))
+        s[i : i + 8] = so
+        c[i : i + 8] = co
+    np.savez_compressed(OUT / "lane_math.npz", sqrt_in=v, sqrt_out=out, angle=ang, sin=s, cos=c)
+
+    # --- CAPT layout of a small surface cloud (collision/capt.hh:294-365)
+    pts = scenes.surface_pointcloud(51, n_points=3000)
+    lay = ref.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS)
+    np.savez_compressed(OUT / "capt_layout.npz", points=pts, r=np.array([0.012, 0.08, scenes.POINT_RADIUS], np.float32), **lay)
+
+    print("golden fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

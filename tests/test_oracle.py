@@ -1,0 +1,109 @@
+"""The CPU oracle (oracle/port) against the reference's own outputs (tests/golden)."""
+import numpy as np
+import pytest
+
+from conftest import golden, scene_of
+from flips import classify_edges, classify_states
+
+ROBOTS = ["panda", "ur5", "fetch", "baxter"]
+
+
+def test_lane_sqrt_is_the_reference_bit_for_bit(port):
+    g = golden("lane_math")
+    mine = port.sqrt_x86(g["sqrt_in"])
+    ref = g["sqrt_out"]
+    assert np.array_equal(np.isnan(mine), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert np.array_equal(mine[ok].view(np.uint32), ref[ok].view(np.uint32))
+
+
+def test_lane_sincos_close_to_reference(port):
+    g = golden("lane_math")
+    s, c = port.sincos(g["angle"])
+    assert np.abs(s - g["sin"]).max() <= 3e-7
+    assert np.abs(c - g["cos"]).max() <= 3e-7
+
+
+@pytest.mark.parametrize("robot", ROBOTS)
+def test_fk_matches_reference(port, robot):
+    g = golden(f"fk_{robot}")
+    rb = port.robot(robot)
+    for q, ref in zip(g["q"], g["spheres"]):
+        s32 = rb.spheres_f32(q)[: rb.fine]
+        s64 = rb.spheres_f64(q.astype(np.float64))[: rb.fine]
+        assert np.abs(s32 - ref).max() <= 1e-6
+        # sphere centres within 1e-5 m of the FP64 kinematics
+        assert np.abs(s64[:, :3] - ref[:, :3]).max() <= 1e-5
+        assert np.array_equal(s32[:, 3], ref[:, 3])
+
+
+@pytest.mark.parametrize(
+    "name,robot",
+    [("states_panda_scene0", "panda"), ("states_panda_scene1", "panda"), ("states_ur5_scene1", "ur5"),
+     ("states_fetch_scene1", "fetch"), ("states_baxter_scene1", "baxter")],
+)
+def test_state_verdicts_match_reference(port, name, robot):
+    g = golden(name)
+    env = port.env(scene_of(g))
+    rb = port.robot(robot)
+    mine = env.validate_states(rb, g["q"])
+    rep = classify_states(env, rb, g["q"], mine, g["verdict"])
+    assert rep["unexplained"] == [], rep
+    assert rep["flips"] <= max(1, len(g["q"]) // 1000)
+
+
+def test_environment_order_matches_reference(port):
+    g = golden("states_panda_scene1")
+    env = port.env(scene_of(g))
+    for k in range(5):
+        mine, ref = env.objects(k), g[f"kind{k}"]
+        assert mine.shape == ref.shape
+        assert np.array_equal(mine[:, :-1], ref[:, :-1])  # same objects in the same order
+        if len(ref):
+            assert np.abs(mine[:, -1] - ref[:, -1]).max() <= 5e-7  # min_distance
+
+
+@pytest.mark.parametrize(
+    "name,robot",
+    [("edges_panda_scene1_res32", "panda"), ("edges_panda_scene0_res1", "panda"), ("edges_panda_scene1_res8", "panda"),
+     ("edges_ur5_scene1_res32", "ur5"), ("edges_fetch_scene1_res32", "fetch"), ("edges_baxter_scene1_res64", "baxter")],
+)
+def test_edge_verdicts_match_reference(port, name, robot):
+    g = golden(name)
+    env = port.env(scene_of(g))
+    rb = port.robot(robot)
+    res = int(g["resolution"])
+    mine, _ = env.validate_motions(rb, g["a"], g["b"], res)
+    rep = classify_edges(env, rb, g["a"], g["b"], res, mine, g["verdict"])
+    assert rep["unexplained"] == [], rep
+    assert rep["flips"] <= max(1, len(g["a"]) // 500)
+
+
+def test_motion_states_are_the_reference_bit_for_bit(port):
+    from flips import motion_states
+
+    g = golden("motion_blocks_panda")
+    rb = port.robot("panda")
+    off = 0
+    for a, b, n in zip(g["a"], g["b"], g["counts"]):
+        ref = g["blocks"][off : off + n]
+        off += n
+        mine = motion_states(rb, a, b, 32).reshape(n, 8, 7)
+        assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+def test_capt_layout_is_the_reference_bit_for_bit(port):
+    g = golden("capt_layout")
+    lay = port.capt(g["points"], *map(float, g["r"]))
+    assert lay["nlog2"] == int(g["nlog2"])
+    for k in ("tests", "aabbs", "aff_starts", "aff", "top"):
+        assert np.array_equal(lay[k], g[k], equal_nan=True), k
+
+
+def test_threads_do_not_change_verdicts(port):
+    g = golden("edges_panda_scene1_res32")
+    env = port.env(scene_of(g))
+    rb = port.robot("panda")
+    one, b1 = env.validate_motions(rb, g["a"], g["b"], 32, threads=1)
+    many, b4 = env.validate_motions(rb, g["a"], g["b"], 32, threads=4)
+    assert np.array_equal(one, many) and np.array_equal(b1, b4)

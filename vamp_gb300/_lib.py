@@ -1,0 +1,95 @@
+"""ctypes binding of libvamp_gb300.so (the C ABI in include/vamp_gb300.h).
+
+The shared library is built in tree (python -m vamp_gb300.build).  There is no fallback: if the
+library is missing, importing vamp_gb300 raises, and if no GPU is usable every check raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvamp_gb300.so"
+
+VG_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state", -5: "limit exceeded"}
+SQRT_X86, SQRT_EXACT = 0, 1
+
+_p = ctypes.c_void_p
+_f = ctypes.c_float
+_i = ctypes.c_int
+_sz = ctypes.c_size_t
+_s = ctypes.c_char_p
+
+
+class VampError(RuntimeError):
+    pass
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build the CUDA library first (python -m vamp_gb300.build). "
+            "vamp_gb300 has no CPU fallback."
+        )
+    lib = ctypes.CDLL(str(LIB_PATH))
+    sig = {
+        "vg_last_error": ([], _s),
+        "vg_version": ([], _s),
+        "vg_robot_info": ([_s, _p, _p, _p, _p, _p], _i),
+        "vg_robot_limits": ([_s, _p, _p], _i),
+        "vg_env_create": ([], _p),
+        "vg_env_destroy": ([_p], None),
+        "vg_env_add_sphere": ([_p, _p], _i),
+        "vg_env_add_capsule": ([_p, _p], _i),
+        "vg_env_add_cuboid": ([_p, _p], _i),
+        "vg_env_set_mode": ([_p, _i, _i], _i),
+        "vg_env_count": ([_p, _i, _p], _i),
+        "vg_env_get": ([_p, _i, _sz, _p], _i),
+        "vg_validate_states_device": ([_s, _p, _p, _sz, _p, _p], _i),
+        "vg_validate_motions_device": ([_s, _p, _p, _p, _sz, _i, _p, _p, _p], _i),
+        "vg_sphere_fk_device": ([_s, _p, _sz, _p, _p], _i),
+        "vg_validate_states": ([_s, _p, _p, _sz, _p], _i),
+        "vg_validate_motions": ([_s, _p, _p, _p, _sz, _i, _p], _i),
+        "vg_sphere_fk": ([_s, _p, _sz, _p], _i),
+        "vg_host_alloc": ([_sz], _p),
+        "vg_host_free": ([_p], None),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+lib = _load()
+
+
+def check(rc: int) -> None:
+    if rc != VG_OK:
+        msg = lib.vg_last_error().decode(errors="replace")
+        raise VampError(f"{ERRORS.get(rc, 'error')} ({rc}): {msg}")
+
+
+# Symbols declared in include/vamp_gb300.h (the C-ABI test checks that each one is exported).
+EXPORTED = (
+    "vg_last_error",
+    "vg_version",
+    "vg_robot_info",
+    "vg_robot_limits",
+    "vg_env_create",
+    "vg_env_destroy",
+    "vg_env_add_sphere",
+    "vg_env_add_capsule",
+    "vg_env_add_cuboid",
+    "vg_env_set_mode",
+    "vg_env_count",
+    "vg_env_get",
+    "vg_validate_states_device",
+    "vg_validate_motions_device",
+    "vg_sphere_fk_device",
+    "vg_validate_states",
+    "vg_validate_motions",
+    "vg_sphere_fk",
+    "vg_host_alloc",
+    "vg_host_free",
+)

@@ -1,0 +1,238 @@
+"""The Python API of vamp_gb300 (loaded on first use by the package).
+
+The Python surface mirrors the reference's bindings (src/impl/vamp/bindings/robot_helper.hh and
+environment.cc): an `Environment` built from primitives, and one submodule per robot with
+`validate`, `validate_motion`, `fk`, `min_max_radii`, `dimension`, `resolution`.  Batched
+forms (`validate_batch`, `validate_motion_batch`) check many configurations or edges in one GPU
+launch; they accept numpy arrays (host) or CUDA torch tensors (device, current stream).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import SQRT_EXACT, SQRT_X86, VampError, check, lib
+
+__all__ = [
+    "Environment",
+    "Robot",
+    "VampError",
+    "SQRT_X86",
+    "SQRT_EXACT",
+    "panda",
+    "ur5",
+    "fetch",
+    "baxter",
+    "ROBOTS",
+]
+
+_p = ctypes.c_void_p
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_p)
+
+
+class Environment:
+    """collision::Environment<float> (src/impl/vamp/collision/environment.hh:15-85).
+
+    Primitive fields follow the reference structs (collision/shapes.hh):
+      sphere  x y z r
+      capsule x1 y1 z1 xv yv zv r rdv   (rdv = 1 / (v . v))
+      cuboid  centre, axis_1, axis_2, axis_3, half extents (15 floats)
+    Objects are kept sorted by their distance to the origin, as the reference sorts them.
+    """
+
+    KINDS = ("spheres", "capsules", "z_aligned_capsules", "cuboids", "z_aligned_cuboids")
+
+    def __init__(self, lanes: int = 8, sqrt_mode: int = SQRT_X86):
+        self._h = lib.vg_env_create()
+        if not self._h:
+            raise VampError("vg_env_create failed")
+        self.set_mode(lanes, sqrt_mode)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.vg_env_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_mode(self, lanes: int, sqrt_mode: int) -> None:
+        """Which reference build to reproduce: (8, SQRT_X86) for AVX2, (4, SQRT_EXACT) for NEON."""
+        check(lib.vg_env_set_mode(self._h, lanes, sqrt_mode))
+        self.lanes, self.sqrt_mode = lanes, sqrt_mode
+
+    def add_sphere(self, sphere) -> None:
+        f = np.ascontiguousarray(_fields(sphere, ("x", "y", "z", "r")), np.float32)
+        check(lib.vg_env_add_sphere(self._h, _ptr(f)))
+
+    def add_capsule(self, capsule) -> None:
+        f = np.ascontiguousarray(_fields(capsule, ("x1", "y1", "z1", "xv", "yv", "zv", "r", "rdv")), np.float32)
+        check(lib.vg_env_add_capsule(self._h, _ptr(f)))
+
+    add_cylinder = add_capsule
+
+    def add_cuboid(self, cuboid) -> None:
+        names = ("x", "y", "z", "axis_1_x", "axis_1_y", "axis_1_z", "axis_2_x", "axis_2_y", "axis_2_z",
+                 "axis_3_x", "axis_3_y", "axis_3_z", "axis_1_r", "axis_2_r", "axis_3_r")
+        f = np.ascontiguousarray(_fields(cuboid, names), np.float32)
+        check(lib.vg_env_add_cuboid(self._h, _ptr(f)))
+
+    @classmethod
+    def from_scene(cls, scene: dict, lanes: int = 8, sqrt_mode: int = SQRT_X86) -> "Environment":
+        env = cls(lanes, sqrt_mode)
+        for s in np.asarray(scene.get("spheres", np.zeros((0, 4))), np.float32):
+            env.add_sphere(s)
+        for c in np.asarray(scene.get("capsules", np.zeros((0, 8))), np.float32):
+            env.add_capsule(c)
+        for c in np.asarray(scene.get("cuboids", np.zeros((0, 15))), np.float32):
+            env.add_cuboid(c)
+        if scene.get("pointclouds"):
+            raise VampError("pointclouds are not supported by this build")
+        return env
+
+    def objects(self, kind: int) -> np.ndarray:
+        """Fields of every object of a kind in checking order, min_distance last."""
+        n = ctypes.c_size_t()
+        check(lib.vg_env_count(self._h, kind, ctypes.byref(n)))
+        width = [5, 9, 9, 16, 16][kind]
+        out = np.zeros((n.value, width), np.float32)
+        for i in range(n.value):
+            check(lib.vg_env_get(self._h, kind, i, _ptr(out[i])))
+        return out
+
+
+def _fields(obj, names):
+    if hasattr(obj, names[0]):
+        return [getattr(obj, n) for n in names]
+    a = np.asarray(obj, np.float32).reshape(-1)
+    if a.size != len(names):
+        raise ValueError(f"expected {len(names)} fields, got {a.size}")
+    return a
+
+
+def _is_cuda_tensor(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+class Robot:
+    """One robot's entry points, mirroring the reference's per-robot Python submodule
+    (bindings/robot_helper.hh:349-648)."""
+
+    def __init__(self, name: str):
+        self.name = name
+        self._b = name.encode()
+        d, n, rmin, rmax, res = ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
+        check(lib.vg_robot_info(self._b, ctypes.byref(d), ctypes.byref(n), ctypes.byref(rmin), ctypes.byref(rmax), ctypes.byref(res)))
+        self._dim, self._n, self._rmin, self._rmax, self._res = d.value, n.value, rmin.value, rmax.value, res.value
+        self.s_m = np.zeros(self._dim, np.float32)
+        self.s_a = np.zeros(self._dim, np.float32)
+        check(lib.vg_robot_limits(self._b, _ptr(self.s_m), _ptr(self.s_a)))
+
+    # constants ---------------------------------------------------------------------------
+    def dimension(self) -> int:
+        return self._dim
+
+    def n_spheres(self) -> int:
+        return self._n
+
+    def resolution(self) -> int:
+        return self._res
+
+    def min_max_radii(self) -> tuple:
+        return self._rmin, self._rmax
+
+    def scale_configuration(self, u):
+        return (np.asarray(u, np.float32) * self.s_m + self.s_a).astype(np.float32)
+
+    def descale_configuration(self, q):
+        return ((np.asarray(q, np.float32) - self.s_a) / self.s_m).astype(np.float32)
+
+    def _in_bounds(self, q) -> bool:
+        u = self.descale_configuration(q)
+        return bool(np.all(u <= 1.0) and np.all(u >= 0.0))
+
+    # single checks (reference semantics) ---------------------------------------------------
+    def validate(self, configuration, environment: Environment, check_bounds: bool = False) -> bool:
+        """Robot validity of one configuration (bindings/robot_helper.hh:256-267)."""
+        q = np.ascontiguousarray(configuration, np.float32).reshape(1, self._dim)
+        if check_bounds and not self._in_bounds(q[0]):
+            return False
+        return bool(self.validate_batch(q, environment)[0])
+
+    def validate_motion(self, configuration_in, configuration_out, environment: Environment,
+                        check_bounds: bool = True, resolution: int = 1) -> bool:
+        """Straight-line motion validity (bindings/robot_helper.hh:269-290).  The Python binding
+        of the reference checks at resolution 1; planners use the robot's resolution()."""
+        a = np.ascontiguousarray(configuration_in, np.float32).reshape(1, self._dim)
+        b = np.ascontiguousarray(configuration_out, np.float32).reshape(1, self._dim)
+        if check_bounds and not (self._in_bounds(a[0]) and self._in_bounds(b[0])):
+            return False
+        return bool(self.validate_motion_batch(a, b, environment, resolution)[0])
+
+    def fk(self, configuration) -> np.ndarray:
+        """Fine sphere centres and radii [n_spheres, 4] (Robot::sphere_fk)."""
+        return self.fk_slots(np.asarray(configuration, np.float32).reshape(1, self._dim))[0, : self._n]
+
+    # batched checks -----------------------------------------------------------------------
+    def validate_batch(self, configurations, environment: Environment, out=None):
+        """Validity of every configuration; numpy in -> numpy uint8 out, CUDA tensor in -> CUDA
+        uint8 tensor out (asynchronous on the current stream)."""
+        if _is_cuda_tensor(configurations):
+            import torch
+
+            q = configurations.contiguous()
+            n = q.shape[0]
+            out = torch.empty(n, dtype=torch.uint8, device=q.device) if out is None else out
+            check(lib.vg_validate_states_device(self._b, environment.handle, q.data_ptr(), n, out.data_ptr(),
+                                                torch.cuda.current_stream(q.device).cuda_stream))
+            return out
+        q = np.ascontiguousarray(configurations, np.float32).reshape(-1, self._dim)
+        out = np.zeros(len(q), np.uint8) if out is None else out
+        check(lib.vg_validate_states(self._b, environment.handle, _ptr(q), len(q), _ptr(out)))
+        return out
+
+    def validate_motion_batch(self, starts, goals, environment: Environment, resolution: int | None = None,
+                              out=None, blocks=None):
+        """Validity of every edge starts[i] -> goals[i] at `resolution` (default: the robot's)."""
+        res = self._res if resolution is None else int(resolution)
+        if _is_cuda_tensor(starts):
+            import torch
+
+            a, b = starts.contiguous(), goals.contiguous()
+            n = a.shape[0]
+            out = torch.empty(n, dtype=torch.uint8, device=a.device) if out is None else out
+            bp = blocks.data_ptr() if blocks is not None else None
+            check(lib.vg_validate_motions_device(self._b, environment.handle, a.data_ptr(), b.data_ptr(), n, res,
+                                                 out.data_ptr(), bp, torch.cuda.current_stream(a.device).cuda_stream))
+            return out
+        a = np.ascontiguousarray(starts, np.float32).reshape(-1, self._dim)
+        b = np.ascontiguousarray(goals, np.float32).reshape(-1, self._dim)
+        out = np.zeros(len(a), np.uint8) if out is None else out
+        check(lib.vg_validate_motions(self._b, environment.handle, _ptr(a), _ptr(b), len(a), res, _ptr(out)))
+        return out
+
+    def fk_slots(self, configurations) -> np.ndarray:
+        """Every sphere slot (fine spheres, then each checked link's coarse sphere) [n, slots, 4]."""
+        q = np.ascontiguousarray(configurations, np.float32).reshape(-1, self._dim)
+        slots = self._slots()
+        out = np.zeros((len(q), slots, 4), np.float32)
+        check(lib.vg_sphere_fk(self._b, _ptr(q), len(q), _ptr(out)))
+        return out
+
+    def _slots(self) -> int:
+        from .robots import slot_count
+
+        return slot_count(self.name)
+
+
+ROBOTS = ("panda", "ur5", "fetch", "baxter")
+panda = Robot("panda")
+ur5 = Robot("ur5")
+fetch = Robot("fetch")
+baxter = Robot("baxter")

@@ -1,0 +1,565 @@
+// C ABI of libvamp_gb300.so (declared in include/vamp_gb300.h).
+//
+// Host code in this file is compiled with -ffp-contract=off: the min_distance of each primitive
+// is computed with explicit fused multiply-adds in the same order as the CPU oracle, so that the
+// GPU and the oracle take identical early-exit decisions.
+#include "../../include/vamp_gb300.h"
+#include "vg_internal.h"
+#include "x86_rsqrt_table.h"
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace vg
+{
+    extern const RobotOps ops_panda;
+    extern const RobotOps ops_ur5;
+    extern const RobotOps ops_fetch;
+    extern const RobotOps ops_baxter;
+
+    const RobotOps *const *all_robots(int *count)
+    {
+        static const RobotOps *const robots[] = {&ops_panda, &ops_ur5, &ops_fetch, &ops_baxter};
+        *count = 4;
+        return robots;
+    }
+
+    const RobotOps *find_robot(const char *name)
+    {
+        if (!name)
+        {
+            return nullptr;
+        }
+        int n = 0;
+        const RobotOps *const *r = all_robots(&n);
+        for (int i = 0; i < n; ++i)
+        {
+            if (std::strcmp(r[i]->name, name) == 0)
+            {
+                return r[i];
+            }
+        }
+        return nullptr;
+    }
+
+    static thread_local std::string g_error;
+
+    int set_error(int code, const std::string &msg)
+    {
+        g_error = msg;
+        return code;
+    }
+
+    static int cuda_fail(cudaError_t e, const char *what)
+    {
+        return set_error(VG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+
+#define VG_CUDA(call, what)                 \
+    do                                      \
+    {                                       \
+        const cudaError_t _e = (call);      \
+        if (_e != cudaSuccess)              \
+        {                                   \
+            return cuda_fail(_e, what);     \
+        }                                   \
+    } while (0)
+
+    // ---------------------------------------------------------------- primitive bookkeeping
+
+    constexpr int kFields[5] = {4, 8, 8, 15, 15};
+
+    static float norm3(float x, float y, float z)
+    {
+        return std::sqrt(std::fma(z, z, std::fma(x, x, y * y)));
+    }
+
+    static void insert_sorted(std::vector<float> &v, int width, const float *row)
+    {
+        // rows are `width` fields + min_distance; keep ascending min_distance, ties after existing
+        const int w = width + 1;
+        size_t pos = v.size() / w;
+        v.resize(v.size() + w);
+        while (pos > 0 && v[(pos - 1) * w + width] > row[width])
+        {
+            std::memcpy(&v[pos * w], &v[(pos - 1) * w], sizeof(float) * w);
+            --pos;
+        }
+        std::memcpy(&v[pos * w], row, sizeof(float) * w);
+    }
+
+    // Sphere::min_distance (collision/shapes.hh:236-240)
+    static float sphere_min_distance(const float *f)
+    {
+        return norm3(f[0], f[1], f[2]) - f[3];
+    }
+
+    // Cylinder::compute_min_distance (collision/shapes.hh:165-189)
+    static float capsule_min_distance(const float *f)
+    {
+        const float x1 = f[0], y1 = f[1], z1 = f[2], xv = f[3], yv = f[4], zv = f[5], r = f[6], rdv = f[7];
+        float t = std::fma(-z1, zv, std::fma(-y1, yv, (-x1) * xv)) * rdv;
+        t = std::fmax(std::fmin(t, 1.0f), 0.0f);
+        const float xp = std::fma(xv, t, x1), yp = std::fma(yv, t, y1), zp = std::fma(zv, t, z1);
+        float xo = -xp, yo = -yp, zo = -zp;
+        const float ol = norm3(xo, yo, zo);
+        xo = xo / ol;
+        yo = yo / ol;
+        zo = zo / ol;
+        const float ro = std::fmax(std::fmin(ol, r), 0.0f);
+        return norm3(std::fma(ro, xo, xp), std::fma(ro, yo, yp), std::fma(ro, zo, zp));
+    }
+
+    // Cuboid::compute_min_distance (collision/shapes.hh:52-67)
+    static float cuboid_min_distance(const float *f)
+    {
+        const float x = f[0], y = f[1], z = f[2];
+        float v[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            const float ax = f[3 + 3 * k], ay = f[4 + 3 * k], az = f[5 + 3 * k], hr = f[12 + k];
+            const float d = std::fma(-z, az, std::fma(-y, ay, (-x) * ax));
+            v[k] = d < -hr ? -hr : (hr < d ? hr : d);
+        }
+        const float xn = std::fma(f[9], v[2], std::fma(f[6], v[1], std::fma(f[3], v[0], x)));
+        const float yn = std::fma(f[10], v[2], std::fma(f[7], v[1], std::fma(f[4], v[0], y)));
+        const float zn = std::fma(f[11], v[2], std::fma(f[8], v[1], std::fma(f[5], v[0], z)));
+        return norm3(xn, yn, zn);
+    }
+
+    // Packs the sorted host rows into the device image (layouts in vg_check.cuh).
+    static void pack_image(const vg_env *e, std::vector<float4> &img, int off[5], int n[5])
+    {
+        img.assign(kRsqrtF4, make_float4(0, 0, 0, 0));
+        std::memcpy(img.data(), kX86RsqrtTable, sizeof(uint32_t) * 2048);
+        for (int k = 0; k < 5; ++k)
+        {
+            const int w = kFields[k] + 1;
+            n[k] = static_cast<int>(e->obj[k].size() / w);
+            off[k] = static_cast<int>(img.size());
+            for (int i = 0; i < n[k]; ++i)
+            {
+                const float *f = &e->obj[k][i * w];
+                const float md = f[kFields[k]];
+                if (k == 0)
+                {
+                    img.push_back(make_float4(f[0], f[1], f[2], f[3]));
+                    img.push_back(make_float4(md, 0, 0, 0));
+                }
+                else if (k <= 2)
+                {
+                    img.push_back(make_float4(f[0], f[1], f[2], f[3]));
+                    img.push_back(make_float4(f[4], f[5], f[6], f[7]));
+                    img.push_back(make_float4(md, 0, 0, 0));
+                }
+                else
+                {
+                    img.push_back(make_float4(f[0], f[1], f[2], f[12]));
+                    img.push_back(make_float4(f[3], f[4], f[5], f[13]));
+                    img.push_back(make_float4(f[6], f[7], f[8], f[14]));
+                    img.push_back(make_float4(f[9], f[10], f[11], md));
+                }
+            }
+        }
+    }
+
+    // Uploads the environment image if it changed; records the current device.
+    static int commit(vg_env *e)
+    {
+        int dev = 0;
+        VG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+        if (!e->dirty && e->d_image && dev == e->device)
+        {
+            return VG_OK;
+        }
+        if (e->d_image && dev != e->device)
+        {
+            return set_error(VG_ERR_STATE, "environment was committed on another device");
+        }
+        std::vector<float4> img;
+        pack_image(e, img, e->off, e->n);
+        if (img.size() > e->image_cap)
+        {
+            if (e->d_image)
+            {
+                cudaFree(e->d_image);
+                e->d_image = nullptr;
+            }
+            VG_CUDA(cudaMalloc(&e->d_image, img.size() * sizeof(float4)), "cudaMalloc(environment)");
+            e->image_cap = img.size();
+        }
+        VG_CUDA(cudaMemcpy(e->d_image, img.data(), img.size() * sizeof(float4), cudaMemcpyHostToDevice), "upload environment");
+        if (!e->d_counter)
+        {
+            VG_CUDA(cudaMalloc(&e->d_counter, 64), "cudaMalloc(counter)");
+        }
+        e->image_f4 = img.size();
+        e->device = dev;
+        e->dirty = false;
+        return VG_OK;
+    }
+
+    static EnvDevice env_device(const vg_env *e)
+    {
+        EnvDevice d{};
+        d.buf = e->d_image;
+        d.n_f4 = static_cast<int>(e->image_f4);
+        for (int k = 0; k < 5; ++k)
+        {
+            d.n[k] = e->n[k];
+            d.off[k] = e->off[k];
+        }
+        d.sqrt_mode = e->sqrt_mode;
+        return d;
+    }
+
+    static int sm_count()
+    {
+        static int count = 0;
+        if (!count)
+        {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+            if (count <= 0)
+            {
+                count = 1;
+            }
+        }
+        return count;
+    }
+
+    static int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm)
+    {
+        if (smem > 48 * 1024)
+        {
+            VG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "cudaFuncSetAttribute");
+        }
+        int occ = 0;
+        VG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, smem), "occupancy");
+        if (occ <= 0)
+        {
+            return set_error(VG_ERR_LIMIT, "kernel does not fit on a multiprocessor (environment too large?)");
+        }
+        *blocks_per_sm = occ;
+        return VG_OK;
+    }
+
+    static int ensure_stage(vg_env *e, size_t bytes)
+    {
+        if (bytes <= e->stage_cap)
+        {
+            return VG_OK;
+        }
+        if (e->d_stage)
+        {
+            cudaFree(e->d_stage);
+            e->d_stage = nullptr;
+            e->stage_cap = 0;
+        }
+        VG_CUDA(cudaMalloc(&e->d_stage, bytes), "cudaMalloc(staging)");
+        e->stage_cap = bytes;
+        return VG_OK;
+    }
+
+    constexpr int kBlock = 128;
+}  // namespace vg
+
+using namespace vg;
+
+extern "C" {
+
+const char *vg_last_error(void)
+{
+    return g_error.c_str();
+}
+
+const char *vg_version(void)
+{
+    return "vamp_gb300 0.1 (sm_103a)";
+}
+
+int vg_robot_info(const char *robot, int *dim, int *n_spheres, float *r_min, float *r_max, int *resolution)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r)
+    {
+        return set_error(VG_ERR_ARG, std::string("unknown robot: ") + (robot ? robot : "(null)"));
+    }
+    if (dim)
+        *dim = r->dim;
+    if (n_spheres)
+        *n_spheres = r->fine;
+    if (r_min)
+        *r_min = r->r_min;
+    if (r_max)
+        *r_max = r->r_max;
+    if (resolution)
+        *resolution = r->resolution;
+    return VG_OK;
+}
+
+int vg_robot_limits(const char *robot, float *s_m, float *s_a)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !s_m || !s_a)
+    {
+        return set_error(VG_ERR_ARG, "vg_robot_limits: unknown robot or null output");
+    }
+    std::memcpy(s_m, r->s_m, sizeof(float) * r->dim);
+    std::memcpy(s_a, r->s_a, sizeof(float) * r->dim);
+    return VG_OK;
+}
+
+vg_env *vg_env_create(void)
+{
+    try
+    {
+        return new vg_env();
+    }
+    catch (...)
+    {
+        set_error(VG_ERR_NOMEM, "vg_env_create: out of memory");
+        return nullptr;
+    }
+}
+
+void vg_env_destroy(vg_env *env)
+{
+    if (!env)
+    {
+        return;
+    }
+    if (env->d_image)
+        cudaFree(env->d_image);
+    if (env->d_counter)
+        cudaFree(env->d_counter);
+    if (env->d_stage)
+        cudaFree(env->d_stage);
+    delete env;
+}
+
+int vg_env_add_sphere(vg_env *env, const float *f)
+{
+    if (!env || !f)
+        return set_error(VG_ERR_ARG, "vg_env_add_sphere: null argument");
+    float row[5] = {f[0], f[1], f[2], f[3], 0.0f};
+    row[4] = sphere_min_distance(f);
+    insert_sorted(env->obj[0], 4, row);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_add_capsule(vg_env *env, const float *f)
+{
+    if (!env || !f)
+        return set_error(VG_ERR_ARG, "vg_env_add_capsule: null argument");
+    float row[9];
+    std::memcpy(row, f, sizeof(float) * 8);
+    row[8] = capsule_min_distance(f);
+    insert_sorted(env->obj[(f[3] == 0.0f && f[4] == 0.0f) ? 2 : 1], 8, row);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_add_cuboid(vg_env *env, const float *f)
+{
+    if (!env || !f)
+        return set_error(VG_ERR_ARG, "vg_env_add_cuboid: null argument");
+    float row[16];
+    std::memcpy(row, f, sizeof(float) * 15);
+    row[15] = cuboid_min_distance(f);
+    insert_sorted(env->obj[f[11] == 1.0f ? 4 : 3], 15, row);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode)
+{
+    if (!env)
+        return set_error(VG_ERR_ARG, "vg_env_set_mode: null environment");
+    if ((lanes != 8 && lanes != 4) || (sqrt_mode != VG_SQRT_X86 && sqrt_mode != VG_SQRT_EXACT))
+    {
+        return set_error(VG_ERR_ARG, "vg_env_set_mode: lanes must be 8 or 4 and sqrt_mode VG_SQRT_X86 or VG_SQRT_EXACT");
+    }
+    env->lanes = lanes;
+    env->sqrt_mode = sqrt_mode;
+    return VG_OK;
+}
+
+int vg_env_count(const vg_env *env, int kind, size_t *count)
+{
+    if (!env || kind < 0 || kind > 4 || !count)
+        return set_error(VG_ERR_ARG, "vg_env_count: bad argument");
+    *count = env->obj[kind].size() / (kFields[kind] + 1);
+    return VG_OK;
+}
+
+int vg_env_get(const vg_env *env, int kind, size_t index, float *out)
+{
+    if (!env || kind < 0 || kind > 4 || !out)
+        return set_error(VG_ERR_ARG, "vg_env_get: bad argument");
+    const size_t w = kFields[kind] + 1;
+    if (index >= env->obj[kind].size() / w)
+        return set_error(VG_ERR_ARG, "vg_env_get: index out of range");
+    std::memcpy(out, &env->obj[kind][index * w], sizeof(float) * w);
+    return VG_OK;
+}
+
+int vg_validate_states_device(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out, void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_validate_states_device: bad argument");
+    if (n == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    int occ = 0;
+    if (int rc = prepare_kernel(r->states_fn, smem, kBlock, &occ))
+        return rc;
+    const long long want = (static_cast<long long>(n) + kBlock - 1) / kBlock;
+    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+    StatesParams p{q, static_cast<long long>(n), out, env_device(env)};
+    VG_CUDA(r->states(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)), "states kernel launch");
+    return VG_OK;
+}
+
+int vg_validate_motions_device(
+    const char *robot,
+    vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!a || !b || !out)) || resolution < 1)
+        return set_error(VG_ERR_ARG, "vg_validate_motions_device: bad argument");
+    if (n > 0x7fffffffu)
+        return set_error(VG_ERR_LIMIT, "vg_validate_motions_device: more than 2^31 - 1 edges");
+    if (n == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int which = env->lanes == 8 ? 0 : 1;
+    int occ = 0;
+    if (int rc = prepare_kernel(r->edges_fn[which], smem, kBlock, &occ))
+        return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
+    const int segs_per_block = kBlock / env->lanes;
+    const long long want = (static_cast<long long>(n) + segs_per_block - 1) / segs_per_block;
+    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env)};
+    VG_CUDA(r->edges[which](p, grid, kBlock, smem, s), "edges kernel launch");
+    return VG_OK;
+}
+
+int vg_sphere_fk_device(const char *robot, const float *q, size_t n, float *out, void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_sphere_fk_device: bad argument");
+    VG_CUDA(r->spheres(q, static_cast<long long>(n), out, static_cast<cudaStream_t>(stream)), "spheres kernel launch");
+    return VG_OK;
+}
+
+int vg_validate_states(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_validate_states: bad argument");
+    if (n == 0)
+        return VG_OK;
+    const size_t qb = n * r->dim * sizeof(float);
+    const size_t qa = (qb + 255) & ~size_t(255);
+    if (int rc = ensure_stage(env, qa + n))
+        return rc;
+    float *dq = static_cast<float *>(env->d_stage);
+    uint8_t *dout = static_cast<uint8_t *>(env->d_stage) + qa;
+    VG_CUDA(cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, 0), "copy configurations");
+    if (int rc = vg_validate_states_device(robot, env, dq, n, dout, nullptr))
+        return rc;
+    VG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, 0), "copy verdicts");
+    VG_CUDA(cudaStreamSynchronize(0), "synchronize");
+    return VG_OK;
+}
+
+int vg_validate_motions(
+    const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution, uint8_t *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!a || !b || !out)))
+        return set_error(VG_ERR_ARG, "vg_validate_motions: bad argument");
+    if (n == 0)
+        return VG_OK;
+    const size_t cb = ((n * r->dim * sizeof(float)) + 255) & ~size_t(255);
+    if (int rc = ensure_stage(env, 2 * cb + n))
+        return rc;
+    char *base = static_cast<char *>(env->d_stage);
+    float *da = reinterpret_cast<float *>(base);
+    float *db = reinterpret_cast<float *>(base + cb);
+    uint8_t *dout = reinterpret_cast<uint8_t *>(base + 2 * cb);
+    VG_CUDA(cudaMemcpyAsync(da, a, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy starts");
+    VG_CUDA(cudaMemcpyAsync(db, b, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy goals");
+    if (int rc = vg_validate_motions_device(robot, env, da, db, n, resolution, dout, nullptr, nullptr))
+        return rc;
+    VG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, 0), "copy verdicts");
+    VG_CUDA(cudaStreamSynchronize(0), "synchronize");
+    return VG_OK;
+}
+
+int vg_sphere_fk(const char *robot, const float *q, size_t n, float *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_sphere_fk: bad argument");
+    if (n == 0)
+        return VG_OK;
+    float *dq = nullptr, *dout = nullptr;
+    const size_t qb = n * r->dim * sizeof(float), ob = n * r->slots * 4 * sizeof(float);
+    VG_CUDA(cudaMalloc(&dq, qb), "cudaMalloc");
+    cudaError_t e = cudaMalloc(&dout, ob);
+    if (e != cudaSuccess)
+    {
+        cudaFree(dq);
+        return cuda_fail(e, "cudaMalloc");
+    }
+    e = cudaMemcpy(dq, q, qb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = r->spheres(dq, static_cast<long long>(n), dout, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, dout, ob, cudaMemcpyDeviceToHost);
+    cudaFree(dq);
+    cudaFree(dout);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "vg_sphere_fk");
+    return VG_OK;
+}
+
+void *vg_host_alloc(size_t bytes)
+{
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess)
+    {
+        set_error(VG_ERR_NOMEM, "cudaMallocHost failed");
+        return nullptr;
+    }
+    return p;
+}
+
+void vg_host_free(void *p)
+{
+    if (p)
+        cudaFreeHost(p);
+}
+
+}  // extern "C"

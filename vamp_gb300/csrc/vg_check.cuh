@@ -1,0 +1,411 @@
+// Device-side collision checking for sm_103a: one configuration per thread, grouped into
+// segments of W consecutive lanes that stand for one SIMD block of the reference.
+//
+// The reference checks W configurations at once in SIMD registers (W = 8 with AVX2, 4 with NEON)
+// and takes some decisions for the whole block (src/impl/vamp/collision/validity.hh:47-150,
+// src/impl/vamp/robots/panda.hh:5630-10259):
+//   * a primitive loop stops only when every lane of the block allows it;
+//   * a test reports a collision when any lane's test value is negative;
+//   * a coarse link sphere that hits in any lane runs the fine tests for every lane.
+// Here those block decisions are warp votes restricted to a segment (__ballot_sync plus bit
+// tricks), and all control flow is warp-uniform: the four 8-lane segments of a warp run the
+// union of their loops, each segment keeping only its own outcomes.  W = 1 gives the reference's
+// single-configuration semantics (its validate() broadcasts one configuration to all lanes).
+//
+// All floating-point operations use explicit round-to-nearest intrinsics so that results are
+// bit-identical with the CPU oracle, which performs the same operations in the same order.
+#pragma once
+
+#include <cstdint>
+
+namespace vg
+{
+    constexpr unsigned kFull = 0xffffffffu;
+
+    enum SqrtMode : int
+    {
+        kSqrtX86 = 0,   // reference built for x86-64: sqrt(v) = v * RSQRTPS(v) (vector/avx.hh:412-415)
+        kSqrtExact = 1  // reference built for Arm: correctly rounded sqrt (vector/neon.hh:520-523)
+    };
+
+    // ------------------------------------------------------------------ segment-wide votes
+
+    // For each W-lane segment: all bits set if any bit of the segment is set in b.
+    template <int W>
+    __device__ __forceinline__ unsigned seg_any(unsigned b)
+    {
+        if constexpr (W == 1)
+        {
+            return b;
+        }
+        else if constexpr (W == 32)
+        {
+            return b ? kFull : 0u;
+        }
+        else if constexpr (W == 8)
+        {
+            const unsigned hi = ((b & 0x7f7f7f7fu) + 0x7f7f7f7fu) | b;  // top bit of each byte: byte != 0
+            return ((hi & 0x80808080u) >> 7) * 0xffu;
+        }
+        else if constexpr (W == 4)
+        {
+            const unsigned hi = ((b & 0x77777777u) + 0x77777777u) | b;  // top bit of each nibble
+            return ((hi & 0x88888888u) >> 3) * 0xfu;
+        }
+        else if constexpr (W == 2)
+        {
+            const unsigned hi = (b | (b >> 1)) & 0x55555555u;
+            return hi * 3u;
+        }
+        else if constexpr (W == 16)
+        {
+            return ((b & 0xffffu) ? 0xffffu : 0u) | ((b >> 16) ? 0xffff0000u : 0u);
+        }
+    }
+
+    template <int W>
+    __device__ __forceinline__ unsigned seg_all(unsigned b)
+    {
+        return ~seg_any<W>(~b);
+    }
+
+    // ---------------------------------------------------------------- scalar arithmetic
+
+    __device__ __forceinline__ int signbit_set(float v)
+    {
+        return __float_as_uint(v) >> 31;
+    }
+
+    // max(v, 0) and clamp(v, 0, 1) with the x86 MAXPS/MINPS operand rule (the second operand is
+    // returned when the comparison fails), as the reference's vector max/clamp compute them.
+    __device__ __forceinline__ float max0(float v)
+    {
+        return v > 0.0f ? v : 0.0f;
+    }
+
+    __device__ __forceinline__ float clamp01(float v)
+    {
+        const float m = v > 0.0f ? v : 0.0f;
+        return m < 1.0f ? m : 1.0f;
+    }
+
+    // sin with the Cephes single-precision method (S. L. Moshier, Cephes Math Library sinf.c),
+    // which the reference uses (vector/avx.hh:456-544); cos(x) = sin(x + pi/2) with arguments
+    // >= pi wrapped by 2 pi (vector/interface.hh:451-458).
+    __device__ __forceinline__ float sin_ref(float x)
+    {
+        unsigned sign = __float_as_uint(x) & 0x80000000u;
+        const float ax = fabsf(x);
+        int j = __float2int_rn(__fmul_rn(ax, 1.27323954473516f));
+        j = (j + 1) & ~1;
+        const float yj = __int2float_rn(j);
+        sign ^= static_cast<unsigned>(j & 4) << 29;
+        float r = __fmaf_rn(yj, -0.78515625f, ax);
+        r = __fmaf_rn(yj, -2.4187564849853515625e-4f, r);
+        r = __fmaf_rn(yj, -3.77489497744594108e-8f, r);
+        const float z = __fmul_rn(r, r);
+
+        float c = __fmaf_rn(2.443315711809948e-5f, z, -1.388731625493765e-3f);
+        c = __fmaf_rn(c, z, 4.166664568298827e-2f);
+        c = __fmul_rn(c, z);
+        c = __fmul_rn(c, z);
+        c = __fmaf_rn(-0.5f, z, c);
+        c = __fadd_rn(c, 1.0f);
+
+        float s = __fmaf_rn(-1.9515295891e-4f, z, 8.3321608736e-3f);
+        s = __fmaf_rn(s, z, -1.6666654611e-1f);
+        s = __fmul_rn(s, z);
+        s = __fmaf_rn(s, r, r);
+
+        const float y = (j & 2) == 0 ? s : c;
+        return __uint_as_float(__float_as_uint(y) ^ sign);
+    }
+
+    __device__ __forceinline__ float cos_ref(float x)
+    {
+        float v = __fadd_rn(x, 1.5707963705062866f);
+        if (v >= 3.14159265359f)
+        {
+            v = __fsub_rn(v, 6.2831854820251465f);
+        }
+        return sin_ref(v);
+    }
+
+    __device__ __forceinline__ void vg_sincos_ref(float x, float *s, float *c)
+    {
+        *s = sin_ref(x);
+        *c = cos_ref(x);
+    }
+
+    // x86 RSQRTPS, from the 2048-entry table of its results on [1, 4): the result depends only on
+    // the exponent parity and the top 10 mantissa bits and scales by powers of four.
+    // Valid for normal positive inputs.
+    __device__ __forceinline__ float rsqrt_x86(const uint32_t *tab, float v)
+    {
+        const unsigned u = __float_as_uint(v);
+        const int E = static_cast<int>(u >> 23) - 127;
+        const int odd = E & 1;
+        const int k = (E - odd) >> 1;
+        const unsigned tb = tab[(static_cast<unsigned>(odd) << 10) | ((u >> 13) & 1023u)];
+        return __uint_as_float((static_cast<unsigned>(static_cast<int>(tb >> 23) - k) << 23) | (tb & 0x7fffffu));
+    }
+
+    // ------------------------------------------------------------------ environment view
+
+    // Record layouts in shared memory (float4 aligned); min_distance is where the primitive loop
+    // reads it first.
+    //   sphere   (2 x float4): x y z r | min_d . . .
+    //   capsule  (3 x float4): x1 y1 z1 xv | yv zv r rdv | min_d . . .
+    //   cuboid   (4 x float4): x y z r1 | a1x a1y a1z r2 | a2x a2y a2z r3 | a3x a3y a3z min_d
+    __host__ __device__ constexpr int rec_f4(int kind)
+    {
+        return kind == 0 ? 2 : (kind <= 2 ? 3 : 4);
+    }
+
+    __host__ __device__ constexpr int min_d_offset(int kind)
+    {
+        return kind == 0 ? 4 : (kind <= 2 ? 8 : 15);
+    }
+
+    struct EnvView
+    {
+        const float4 *rec[5];
+        int n[5];
+        const uint32_t *rsqrt_tab;
+        int sqrt_mode;
+    };
+
+    __device__ __forceinline__ float sql2(float ax, float ay, float az, float bx, float by, float bz)
+    {
+        const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+        return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    }
+
+    // Primitive tests: sign bit set iff the sphere collides (collision/sphere_*.hh).
+    __device__ __forceinline__ float t_sphere(const float4 *o, float x, float y, float z, float r)
+    {
+        const float4 a = o[0];
+        const float rs = __fadd_rn(a.w, r);
+        return __fmaf_rn(-rs, rs, sql2(a.x, a.y, a.z, x, y, z));
+    }
+
+    __device__ __forceinline__ float t_capsule(const float4 *o, float x, float y, float z, float r)
+    {
+        const float4 a = o[0], b = o[1];  // x1 y1 z1 xv | yv zv r rdv
+        const float dot = __fmaf_rn(__fsub_rn(z, a.z), b.y, __fmaf_rn(__fsub_rn(y, a.y), b.x, __fmul_rn(__fsub_rn(x, a.x), a.w)));
+        const float t = clamp01(__fmul_rn(dot, b.w));
+        const float px = __fmaf_rn(a.w, t, a.x), py = __fmaf_rn(b.x, t, a.y), pz = __fmaf_rn(b.y, t, a.z);
+        const float rs = __fadd_rn(r, b.z);
+        return __fmaf_rn(-rs, rs, sql2(x, y, z, px, py, pz));
+    }
+
+    __device__ __forceinline__ float t_zcapsule(const float4 *o, float x, float y, float z, float r)
+    {
+        const float4 a = o[0], b = o[1];
+        const float t = clamp01(__fmul_rn(__fmul_rn(__fsub_rn(z, a.z), b.y), b.w));
+        const float pz = __fmaf_rn(b.y, t, a.z);
+        const float rs = __fadd_rn(r, b.z);
+        return __fmaf_rn(-rs, rs, sql2(x, y, z, a.x, a.y, pz));
+    }
+
+    __device__ __forceinline__ float t_cuboid(const float4 *o, float x, float y, float z, float rsq)
+    {
+        const float4 a = o[0], b = o[1], c = o[2], d = o[3];
+        // a: x y z r1 | b: a1x a1y a1z r2 | c: a2x a2y a2z r3 | d: a3x a3y a3z min_d
+        const float xs = __fsub_rn(x, a.x), ys = __fsub_rn(y, a.y), zs = __fsub_rn(z, a.z);
+        const float a1 = max0(__fsub_rn(fabsf(__fmaf_rn(b.z, zs, __fmaf_rn(b.y, ys, __fmul_rn(b.x, xs)))), a.w));
+        const float a2 = max0(__fsub_rn(fabsf(__fmaf_rn(c.z, zs, __fmaf_rn(c.y, ys, __fmul_rn(c.x, xs)))), b.w));
+        const float a3 = max0(__fsub_rn(fabsf(__fmaf_rn(d.z, zs, __fmaf_rn(d.y, ys, __fmul_rn(d.x, xs)))), c.w));
+        return __fsub_rn(__fmaf_rn(a3, a3, __fmaf_rn(a2, a2, __fmul_rn(a1, a1))), rsq);
+    }
+
+    __device__ __forceinline__ float t_zcuboid(const float4 *o, float x, float y, float z, float rsq)
+    {
+        const float4 a = o[0], b = o[1], c = o[2];
+        const float xs = __fsub_rn(x, a.x), ys = __fsub_rn(y, a.y), zs = __fsub_rn(z, a.z);
+        const float a1 = max0(__fsub_rn(fabsf(__fmaf_rn(b.y, ys, __fmul_rn(b.x, xs))), a.w));
+        const float a2 = max0(__fsub_rn(fabsf(__fmaf_rn(c.y, ys, __fmul_rn(c.x, xs))), b.w));
+        const float a3 = max0(__fsub_rn(fabsf(zs), c.w));
+        return __fsub_rn(__fmaf_rn(a3, a3, __fmaf_rn(a2, a2, __fmul_rn(a1, a1))), rsq);
+    }
+
+    // The early-exit bound max_extent = |c| + r of one lane (validity.hh:56): +inf when the
+    // lane can never allow a stop (|c|^2 zero or subnormal under the x86 rule).
+    __device__ __forceinline__ float max_extent(const EnvView &e, float v, float r)
+    {
+        if (e.sqrt_mode == kSqrtX86)
+        {
+            return v >= 1.17549435e-38f ? __fmaf_rn(v, rsqrt_x86(e.rsqrt_tab, v), r) : __int_as_float(0x7f800000);
+        }
+        return __fadd_rn(__fsqrt_rn(v), r);
+    }
+
+    // One kind's primitive loop for the segments in `scan`; returns the lanes whose segment hit.
+    template <int W, int KIND>
+    __device__ __forceinline__ unsigned kind_loop(
+        const EnvView &e, unsigned scan, float me, float x, float y, float z, float rr)
+    {
+        unsigned hit = 0;
+        const float4 *rec = e.rec[KIND];
+        const int n = e.n[KIND];
+        for (int i = 0; i < n; ++i)
+        {
+            const float4 *o = rec + i * rec_f4(KIND);
+            const float md = reinterpret_cast<const float *>(o)[min_d_offset(KIND)];
+            // the segment stops at this object when every lane's (min_d - max_extent) has a
+            // clear sign bit
+            const unsigned stop = seg_all<W>(__ballot_sync(kFull, !signbit_set(__fsub_rn(md, me))));
+            scan &= ~stop;
+            if (!scan)
+            {
+                break;
+            }
+            float t;
+            if constexpr (KIND == 0)
+                t = t_sphere(o, x, y, z, rr);
+            else if constexpr (KIND == 1)
+                t = t_capsule(o, x, y, z, rr);
+            else if constexpr (KIND == 2)
+                t = t_zcapsule(o, x, y, z, rr);
+            else if constexpr (KIND == 3)
+                t = t_cuboid(o, x, y, z, rr);
+            else
+                t = t_zcuboid(o, x, y, z, rr);
+            const unsigned h = seg_any<W>(__ballot_sync(kFull, signbit_set(t))) & scan;
+            hit |= h;
+            scan &= ~h;
+            if (!scan)
+            {
+                break;
+            }
+        }
+        return hit;
+    }
+
+    // sphere_environment_in_collision (validity.hh:47-150) for the segments in `mask`: returns
+    // the lanes of the segments whose block collides.  Warp-uniform; all 32 lanes must call.
+    template <int W>
+    __device__ __noinline__ unsigned env_query(const EnvView &e, float x, float y, float z, float r, unsigned mask)
+    {
+        const float v = __fmaf_rn(x, x, __fmaf_rn(z, z, __fmul_rn(y, y)));
+        const float me = max_extent(e, v, r);
+        const float rsq = __fmul_rn(r, r);
+        unsigned hit = 0;
+        unsigned todo = mask;
+        unsigned h = kind_loop<W, 0>(e, todo, me, x, y, z, r);
+        hit |= h;
+        todo &= ~h;
+        if (todo)
+        {
+            h = kind_loop<W, 1>(e, todo, me, x, y, z, r);
+            hit |= h;
+            todo &= ~h;
+        }
+        if (todo)
+        {
+            h = kind_loop<W, 2>(e, todo, me, x, y, z, r);
+            hit |= h;
+            todo &= ~h;
+        }
+        if (todo)
+        {
+            h = kind_loop<W, 3>(e, todo, me, x, y, z, rsq);
+            hit |= h;
+            todo &= ~h;
+        }
+        if (todo)
+        {
+            h = kind_loop<W, 4>(e, todo, me, x, y, z, rsq);
+            hit |= h;
+        }
+        return hit;
+    }
+
+    // sphere_sphere_self_collision (validity.hh:23-44) for the segments in `mask`.
+    template <int W>
+    __device__ __forceinline__ unsigned self_query(
+        float ax, float ay, float az, float ar, float bx, float by, float bz, float br, unsigned mask)
+    {
+        const float rs = __fadd_rn(ar, br);
+        const float t = __fmaf_rn(-rs, rs, sql2(ax, ay, az, bx, by, bz));
+        return seg_any<W>(__ballot_sync(kFull, signbit_set(t))) & mask;
+    }
+
+    // The context a generated Robot::fkcc body runs against.
+    template <int W>
+    struct CheckCtx
+    {
+        const EnvView &env;
+        unsigned alive;
+
+        __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
+        {
+            return env_query<W>(env, x, y, z, r, mask);
+        }
+
+        __device__ __forceinline__ unsigned self_hit(
+            float ax, float ay, float az, float ar, float bx, float by, float bz, float br, unsigned mask)
+        {
+            return self_query<W>(ax, ay, az, ar, bx, by, bz, br, mask);
+        }
+    };
+    // Fine environment tests of one link's spheres, in order, for the segments in `need`.
+    // Clears colliding segments from ctx.alive; returns true once none is left.
+    template <int N, typename Ctx>
+    __device__ __forceinline__ bool env_fine(Ctx &ctx, const float4 *s, unsigned need)
+    {
+#pragma unroll 1
+        for (int k = 0; k < N; ++k)
+        {
+            const float4 c = s[k];
+            const unsigned hit = ctx.env_hit(c.x, c.y, c.z, c.w, need);
+            if (hit)
+            {
+                need &= ~hit;
+                ctx.alive &= ~hit;
+                if (!ctx.alive)
+                {
+                    return true;
+                }
+                if (!need)
+                {
+                    return false;
+                }
+            }
+        }
+        return false;
+    }
+
+    // Fine self-collision tests of one link pair: every sphere of link A against every sphere
+    // of link B (the reference's generated pair list is this cross product), for the segments
+    // in `need`.  Clears colliding segments from ctx.alive; returns true once none is left.
+    template <int NA, int NB, typename Ctx>
+    __device__ __forceinline__ bool self_cross(Ctx &ctx, const float4 *sa, const float4 *sb, unsigned need)
+    {
+#pragma unroll 1
+        for (int i = 0; i < NA; ++i)
+        {
+            const float4 a = sa[i];
+#pragma unroll 1
+            for (int j = 0; j < NB; ++j)
+            {
+                const float4 b = sb[j];
+                const unsigned hit = ctx.self_hit(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, need);
+                if (hit)
+                {
+                    need &= ~hit;
+                    ctx.alive &= ~hit;
+                    if (!ctx.alive)
+                    {
+                        return true;
+                    }
+                    if (!need)
+                    {
+                        return false;
+                    }
+                }
+            }
+        }
+        return false;
+    }
+}  // namespace vg

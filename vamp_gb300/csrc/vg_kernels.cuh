@@ -1,0 +1,252 @@
+// Batched collision-checking kernels for sm_103a.
+//
+//   states_kernel : Robot::fkcc for one configuration per thread, as the reference's
+//                   validate(q) evaluates it (bindings/robot_helper.hh:256-267).
+//   edges_kernel  : planning::validate_motion for a batch of edges (planning/validate.hh:24-77).
+//                   Persistent: each W-lane segment owns one edge at a time, walks its blocks in
+//                   the reference's order (block 0 = fractions k/W, then repeated back-steps),
+//                   stops at the first colliding block and pulls the next edge from a global
+//                   counter.  A warp checks four blocks of four different edges per step.
+//   spheres_kernel: all sphere slots for a batch of configurations (Robot::sphere_fk).
+#pragma once
+
+#include <cstdint>
+
+#include "vg_check.cuh"
+
+namespace vg
+{
+    // Device image of an environment: the x86 RSQRTPS table followed by the primitive records
+    // of each kind (layouts in vg_check.cuh), all float4 aligned.
+    struct EnvDevice
+    {
+        const float4 *buf;  // whole image
+        int n_f4;           // image size in float4
+        int n[5];           // objects per kind
+        int off[5];         // record offset of each kind, in float4 from the image start
+        int sqrt_mode;
+    };
+
+    constexpr int kRsqrtF4 = 2048 / 4;
+
+    __device__ __forceinline__ EnvView stage_env(const EnvDevice &d, float4 *smem)
+    {
+        for (int i = threadIdx.x; i < d.n_f4; i += blockDim.x)
+        {
+            smem[i] = d.buf[i];
+        }
+        __syncthreads();
+        EnvView v;
+        v.rsqrt_tab = reinterpret_cast<const uint32_t *>(smem);
+        v.sqrt_mode = d.sqrt_mode;
+        for (int k = 0; k < 5; ++k)
+        {
+            v.rec[k] = smem + d.off[k];
+            v.n[k] = d.n[k];
+        }
+        return v;
+    }
+
+    template <typename Robot, int W>
+    __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive)
+    {
+        CheckCtx<W> ctx{ev, alive};
+        Robot::fkcc(q, ctx);
+        return ctx.alive;
+    }
+
+    // ------------------------------------------------------------------------------ states
+
+    struct StatesParams
+    {
+        const float *q;  // [n][dim]
+        long long n;
+        uint8_t *out;    // 1 = valid
+        EnvDevice env;
+    };
+
+    template <typename Robot>
+    __global__ void __launch_bounds__(128) states_kernel(StatesParams p)
+    {
+        extern __shared__ float4 smem[];
+        const EnvView ev = stage_env(p.env, smem);
+        constexpr int D = Robot::kDim;
+        const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+        // every lane of a warp iterates the same number of times (warp-uniform loop)
+        const long long base0 = static_cast<long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31);
+        for (long long base = base0; base < p.n; base += stride)
+        {
+            const long long idx = base + (threadIdx.x & 31);
+            const bool in = idx < p.n;
+            float q[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                q[d] = in ? p.q[idx * D + d] : 0.0f;
+            }
+            const unsigned alive = run_fkcc<Robot, 1>(ev, q, __ballot_sync(kFull, in));
+            if (in)
+            {
+                p.out[idx] = static_cast<uint8_t>((alive >> (threadIdx.x & 31)) & 1u);
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------------------- edges
+
+    struct EdgesParams
+    {
+        const float *a;  // [n][dim] start configurations
+        const float *b;  // [n][dim] goal configurations
+        int n;
+        int resolution;
+        uint8_t *out;        // 1 = valid
+        int32_t *blocks;     // optional: blocks checked per edge
+        unsigned *head;      // work counter, zero before launch
+        EnvDevice env;
+    };
+
+    // |b - a| as the reference computes it on x86: squares summed lane-wise over the 8-wide
+    // vectors that hold the configuration, then ((s0+s4)+(s2+s6)) + ((s1+s5)+(s3+s7)), then a
+    // correctly rounded sqrt (vector/avx.hh:442-452, vector/interface.hh:402-410).
+    template <int D>
+    __device__ __forceinline__ float edge_length(const float *v)
+    {
+        float s[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            s[k] = 0.0f;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            const float sq = __fmul_rn(v[d], v[d]);
+            s[d & 7] = d < 8 ? sq : __fadd_rn(s[d & 7], sq);
+        }
+        const float a0 = __fadd_rn(s[4], s[0]), a1 = __fadd_rn(s[5], s[1]);
+        const float a2 = __fadd_rn(s[6], s[2]), a3 = __fadd_rn(s[7], s[3]);
+        return __fsqrt_rn(__fadd_rn(__fadd_rn(a0, a2), __fadd_rn(a1, a3)));
+    }
+
+    template <typename Robot, int W>
+    __global__ void __launch_bounds__(128) edges_kernel(EdgesParams p)
+    {
+        extern __shared__ float4 smem[];
+        const EnvView ev = stage_env(p.env, smem);
+        constexpr int D = Robot::kDim;
+        const int lane = threadIdx.x & 31;
+        const int sl = lane % W;                  // lane within the segment
+        const int leader = lane - sl;             // segment's first lane
+        constexpr unsigned kLeaders = W == 1 ? kFull : (W == 2 ? 0x55555555u : (W == 4 ? 0x11111111u : (W == 8 ? 0x01010101u : (W == 16 ? 0x00010001u : 1u))));
+        const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
+
+        int e = -1;       // current edge of my segment (-1: none)
+        int n = 0;        // blocks of the edge
+        int i = 0;        // current block
+        float q[D], bs[D];
+
+        // Pull new edges for the segments in `need` (a lane mask, whole segments).
+        auto refill = [&](unsigned need) {
+            const unsigned lead = need & kLeaders;
+            unsigned base = 0;
+            if (lane == 0)
+            {
+                base = atomicAdd(p.head, static_cast<unsigned>(__popc(lead)));
+            }
+            base = __shfl_sync(kFull, base, 0);
+            const unsigned mine = base + __popc(lead & ((1u << lane) - 1u));
+            const unsigned got = __shfl_sync(kFull, mine, leader);
+            if ((need >> lane) & 1u)
+            {
+                if (got >= static_cast<unsigned>(p.n))
+                {
+                    e = -1;
+                }
+                else
+                {
+                    e = static_cast<int>(got);
+                    float av[D], v[D];
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        av[d] = p.a[static_cast<long long>(e) * D + d];
+                        v[d] = __fsub_rn(p.b[static_cast<long long>(e) * D + d], av[d]);
+                    }
+                    const float len = edge_length<D>(v);
+                    const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
+                    const float nf = ceilf(t);
+                    n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
+                    i = 0;
+                    const float denom = static_cast<float>(W * n);
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        q[d] = __fmaf_rn(v[d], pct, av[d]);
+                        bs[d] = __fdiv_rn(v[d], denom);
+                    }
+                }
+            }
+        };
+
+        refill(kFull);
+        for (;;)
+        {
+            const unsigned active = __ballot_sync(kFull, e >= 0);
+            if (!active)
+            {
+                break;
+            }
+            const unsigned alive = run_fkcc<Robot, W>(ev, q, active);
+            bool finish = false;
+            if (e >= 0)
+            {
+                const bool bad = ((alive >> lane) & 1u) == 0u;
+                if (bad || i + 1 >= n)
+                {
+                    finish = true;
+                    if (sl == 0)
+                    {
+                        p.out[e] = bad ? 0 : 1;
+                        if (p.blocks)
+                        {
+                            p.blocks[e] = i + 1;
+                        }
+                    }
+                }
+                else
+                {
+                    ++i;
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        q[d] = __fsub_rn(q[d], bs[d]);
+                    }
+                }
+            }
+            const unsigned need = __ballot_sync(kFull, finish);
+            if (need)
+            {
+                refill(need);
+            }
+        }
+    }
+
+    // ----------------------------------------------------------------------------- spheres
+
+    template <typename Robot>
+    __global__ void spheres_kernel(const float *q, long long n, float *out)
+    {
+        const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (idx >= n)
+        {
+            return;
+        }
+        float qq[Robot::kDim];
+        for (int d = 0; d < Robot::kDim; ++d)
+        {
+            qq[d] = q[idx * Robot::kDim + d];
+        }
+        Robot::spheres(qq, out + idx * Robot::kSlots * 4);
+    }
+}  // namespace vg

@@ -1,0 +1,64 @@
+// Instantiates the kernels of one robot and describes them to the library (included by
+// robot_<name>.cu after the robot's generated header).
+#pragma once
+
+#include "vg_internal.h"
+
+namespace vg
+{
+    template <typename R>
+    cudaError_t launch_states(const StatesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        states_kernel<R><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
+    template <typename R, int W>
+    cudaError_t launch_edges(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        edges_kernel<R, W><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
+    template <typename R>
+    cudaError_t launch_spheres(const float *q, long long n, float *out, cudaStream_t s)
+    {
+        if (n <= 0)
+        {
+            return cudaSuccess;
+        }
+        const int block = 128;
+        spheres_kernel<R><<<static_cast<unsigned>((n + block - 1) / block), block, 0, s>>>(q, n, out);
+        return cudaGetLastError();
+    }
+
+    template <typename R>
+    RobotOps make_robot_ops()
+    {
+        RobotOps o{};
+        o.name = R::kName;
+        o.dim = R::kDim;
+        o.fine = R::kFine;
+        o.slots = R::kSlots;
+        o.resolution = R::kResolution;
+        o.r_min = R::kMinRadius;
+        o.r_max = R::kMaxRadius;
+        o.s_m = R::kScaleM;
+        o.s_a = R::kScaleA;
+        o.states = &launch_states<R>;
+        o.states_fn = reinterpret_cast<const void *>(&states_kernel<R>);
+        o.edges[0] = &launch_edges<R, 8>;
+        o.edges[1] = &launch_edges<R, 4>;
+        o.edges_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8>);
+        o.edges_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4>);
+        o.spheres = &launch_spheres<R>;
+        return o;
+    }
+}  // namespace vg
+
+#define VG_DEFINE_ROBOT(Type, var)                                                 \
+    namespace vg                                                                   \
+    {                                                                              \
+        extern const RobotOps var;                                                 \
+        const RobotOps var = make_robot_ops<vg::robots::Type>();                   \
+    }

@@ -1,0 +1,757 @@
+"""Straight-line forward-kinematics + collision-schedule generator.
+
+Input: a robot model JSON (vamp_gb300/robots/<robot>.json, written by extract.py).
+Output:
+  * vamp_gb300/csrc/robots/<robot>.cuh  - CUDA device code for sm_103a: FP32 FK of every sphere and
+    the robot's fkcc check schedule, written against a small context interface (see
+    vamp_gb300/csrc/vg_check.cuh);
+  * oracle/port/robots/<robot>.h        - C code for the CPU oracle: the same FP32 FK (bit-identical
+    operation sequence), an FP64 FK for centre tolerances and distance-to-contact, and the check
+    schedule as tables.
+
+Design.  Each movable joint gets one frame (R, t) in registers.  Links attached by fixed joints
+share their moving ancestor's frame; their spheres are re-expressed in that frame at generation
+time (float64, then rounded once to float32).  A frame is the parent frame times a constant
+transform times the joint motion, with exact zeros and ones folded out, so an axis-aligned joint
+costs 12 multiply-adds.  Every floating-point operation is emitted explicitly (fused multiply-add,
+multiply, add) so that the CUDA and C versions round identically: the GPU kernels and the CPU
+oracle compute bit-identical sphere centres.
+
+The reference's generated kernels compute the same kinematics with a different operation order
+(src/impl/vamp/robots/panda.hh:5229-5627), so centres agree with the reference to a few ulp, not
+bit for bit; the FP64 FK bounds that difference.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+
+from .urdf import axis_rotation, rpy_matrix
+
+ROOT = Path(__file__).resolve().parents[2]
+MODELS = ROOT / "vamp_gb300" / "robots"
+CUDA_OUT = ROOT / "vamp_gb300" / "csrc" / "robots"
+C_OUT = ROOT / "oracle" / "port" / "robots"
+
+
+def f32(v: float) -> float:
+    return float(np.float32(v))
+
+
+def lit32(v: float) -> str:
+    v = f32(v)
+    if v == 0.0:
+        return "0.0f"
+    r = repr(v)
+    if "e" not in r and "." not in r:
+        r += ".0"
+    return r + "f"
+
+
+def lit64(v: float) -> str:
+    r = repr(float(v))
+    if "e" not in r and "." not in r and "inf" not in r and "nan" not in r:
+        r += ".0"
+    return r
+
+
+class Emitter:
+    """Emits explicit arithmetic for one target.
+
+    A value is a Python float (a constant, already rounded for the target), a variable name, or a
+    variable name prefixed with '-' (its negation, folded into the operation that uses it).
+    `snap` folds constants within `snap` of 0 or +-1 to exact values (float targets only).
+    """
+
+    def __init__(self, target: str, snap: float):
+        self.target = target  # "cuda" | "c32" | "c64"
+        self.snap = snap
+        self.lines: list[str] = []
+        self.n = 0
+        self.ty = "double" if target == "c64" else "float"
+        self.flops = 0  # floating-point operations emitted (a fused multiply-add counts 2)
+
+    def const(self, v: float) -> float:
+        if self.snap:
+            if abs(v) < self.snap:
+                v = 0.0
+            elif abs(v - 1.0) < self.snap:
+                v = 1.0
+            elif abs(v + 1.0) < self.snap:
+                v = -1.0
+        return float(v) if self.target == "c64" else f32(v)
+
+    def lit(self, v) -> str:
+        return lit64(v) if self.target == "c64" else lit32(v)
+
+    def ref(self, v) -> str:
+        if isinstance(v, float):
+            return self.lit(v)
+        return f"(-{v[1:]})" if v.startswith("-") else v
+
+    def _fma(self, a, b, c) -> str:
+        self.flops += 2
+        a, b, c = self.ref(a), self.ref(b), self.ref(c)
+        if self.target == "cuda":
+            return f"__fmaf_rn({a}, {b}, {c})"
+        return f"{'fma' if self.target == 'c64' else 'fmaf'}({a}, {b}, {c})"
+
+    def _mul(self, a, b) -> str:
+        self.flops += 1
+        a, b = self.ref(a), self.ref(b)
+        return f"__fmul_rn({a}, {b})" if self.target == "cuda" else f"({a} * {b})"
+
+    def _add(self, a, b) -> str:
+        self.flops += 1
+        a, b = self.ref(a), self.ref(b)
+        return f"__fadd_rn({a}, {b})" if self.target == "cuda" else f"({a} + {b})"
+
+    def assign(self, expr: str, name: str | None = None) -> str:
+        if name is None:
+            name = f"_v{self.n}"
+            self.n += 1
+        self.lines.append(f"const {self.ty} {name} = {expr};")
+        return name
+
+    @staticmethod
+    def _neg(v):
+        if isinstance(v, float):
+            return -v
+        return v[1:] if v.startswith("-") else "-" + v
+
+    def lincomb(self, terms, const=0.0, name=None):
+        """Emit const + sum(coef * a * b) for terms (coef, a, b|None).  Returns a value.
+
+        Order: the constant (if non-zero) starts the accumulator, then each product is fused
+        in turn; a lone product starts with a multiply.
+        """
+        prods = []
+        c0 = const
+        for coef, a, b in terms:
+            k = coef
+            vs = []
+            for x in (a, b):
+                if x is None:
+                    continue
+                if isinstance(x, float):
+                    k *= x
+                else:
+                    if x.startswith("-"):
+                        k = -k
+                        x = x[1:]
+                    vs.append(x)
+            k = self.const(k)
+            if k == 0.0:
+                continue
+            if not vs:
+                c0 += k
+                continue
+            prods.append((k, vs))
+        c0 = self.const(c0)
+        if not prods:
+            return c0
+        # start the accumulator from a bare variable when there is one (saves an operation)
+        if c0 == 0.0:
+            for i, (k, vs) in enumerate(prods):
+                if len(vs) == 1 and k in (1.0, -1.0):
+                    prods.insert(0, prods.pop(i))
+                    break
+
+        def operand(k, vs):
+            # returns (x, y) with x * y == k * prod(vs); may emit one multiply for 3-factor terms
+            if len(vs) == 1:
+                if k == 1.0:
+                    return None, vs[0]
+                if k == -1.0:
+                    return None, "-" + vs[0]
+                return k, vs[0]
+            if k == 1.0:
+                return vs[0], vs[1]
+            if k == -1.0:
+                return "-" + vs[0], vs[1]
+            t = self.assign(self._mul(k, vs[0]))
+            return t, vs[1]
+
+        if c0 != 0.0:
+            acc = c0
+            rest = prods
+        else:
+            x, y = operand(*prods[0])
+            if x is None:
+                acc = y
+            else:
+                acc = self.assign(self._mul(x, y))
+            rest = prods[1:]
+        for k, vs in rest:
+            x, y = operand(k, vs)
+            if x is None:
+                if y.startswith("-"):
+                    acc = self.assign(self._add(acc, y))  # acc + (-y)
+                else:
+                    acc = self.assign(self._add(acc, y))
+            else:
+                acc = self.assign(self._fma(x, y, acc))
+        if name is not None and isinstance(acc, str):
+            last = self.lines[-1] if self.lines else ""
+            if acc.startswith("_v") and last.startswith(f"const {self.ty} {acc} ="):
+                self.lines[-1] = last.replace(f"const {self.ty} {acc} =", f"const {self.ty} {name} =", 1)
+                return name
+            return self.assign(self.ref(acc), name)
+        return acc
+
+
+# --------------------------------------------------------------------------------------------
+# kinematic structure
+
+
+class Kin:
+    """Frames of a robot: one per movable joint plus the root, with fixed links folded."""
+
+    def __init__(self, model: dict):
+        self.m = model
+        joints = model["joints"]
+        self.by_child = {j["child"]: j for j in joints}
+        self.jindex = {n: i for i, n in enumerate(model["joint_names"])}
+        # frame of every link: (frame_id, constant 4x4 from frame to link)
+        self.link_frame = {model["root"]: ("root", np.eye(4))}
+        self.frames = []  # movable frames in topological order: dict
+        pending = list(joints)
+        while pending:
+            rest = []
+            for j in pending:
+                if j["parent"] not in self.link_frame:
+                    rest.append(j)
+                    continue
+                fid, C = self.link_frame[j["parent"]]
+                O = np.eye(4)
+                O[:3, :3] = rpy_matrix(j["rpy"])
+                O[:3, 3] = j["xyz"]
+                K = C @ O
+                if j["type"] == "fixed" or j["name"] not in self.jindex:
+                    if j["type"] != "fixed":
+                        # a movable joint the configuration does not drive: hold it at zero
+                        pass
+                    self.link_frame[j["child"]] = (fid, K)
+                else:
+                    name = f"F{len(self.frames)}"
+                    self.frames.append(
+                        {
+                            "id": name,
+                            "parent": fid,
+                            "K": K,
+                            "axis": np.asarray(j["axis"], dtype=np.float64),
+                            "type": j["type"],
+                            "q": self.jindex[j["name"]],
+                            "joint": j["name"],
+                        }
+                    )
+                    self.link_frame[j["child"]] = (name, np.eye(4))
+            assert len(rest) < len(pending)
+            pending = rest
+
+    def sphere_in_frame(self, link: str, p) -> tuple:
+        fid, C = self.link_frame[link]
+        v = C @ np.array([p[0], p[1], p[2], 1.0])
+        return fid, v[:3]
+
+
+def emit_frames(kin: Kin, em: Emitter, qname="q", sc_fn=None):
+    """Emit every movable frame; returns {frame_id: (R, t)} with values (floats or names)."""
+    frames = {"root": ([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]], [0.0, 0.0, 0.0])}
+    for f in kin.frames:
+        Rp, tp = frames[f["parent"]]
+        K = f["K"]
+        fid = f["id"]
+        # fixed part: M = Rp @ K_R, t0 = tp + Rp @ K_t
+        t0 = [em.lincomb([(float(K[k, 3]), Rp[r][k], None) for k in range(3)] + [(1.0, tp[r], None)]) for r in range(3)]
+        M = [[em.lincomb([(float(K[k, c]), Rp[r][k], None) for k in range(3)]) for c in range(3)] for r in range(3)]
+        axis = f["axis"] / np.linalg.norm(f["axis"])
+        qv = f"{qname}[{f['q']}]"
+        if f["type"] in ("revolute", "continuous"):
+            s, c = f"{fid}_s", f"{fid}_c"
+            em.lines.append(sc_fn(qv, s, c))
+            # joint rotation (Rodrigues): Rj = c (I - a a^T) + s [a]x + a a^T
+            kx = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+            aa = np.outer(axis, axis)
+            R = []
+            for r in range(3):
+                row = []
+                for cc in range(3):
+                    terms = []
+                    for k in range(3):
+                        terms.append(((1.0 if k == cc else 0.0) - aa[k, cc], M[r][k], c))
+                        terms.append((kx[k, cc], M[r][k], s))
+                        terms.append((aa[k, cc], M[r][k], None))
+                    row.append(em.lincomb(terms, 0.0, name=f"{fid}_r{r}{cc}"))
+                R.append(row)
+            t = [em.lincomb([(1.0, t0[r], None)], 0.0, name=f"{fid}_t{r}") for r in range(3)]
+        elif f["type"] == "prismatic":
+            R = M
+            t = [
+                em.lincomb(
+                    [(1.0, t0[r], None)] + [(float(axis[k]), M[r][k], qv) for k in range(3)],
+                    0.0,
+                    name=f"{fid}_t{r}",
+                )
+                for r in range(3)
+            ]
+        else:
+            raise ValueError(f["type"])
+        frames[fid] = (R, t)
+    return frames
+
+
+def emit_centre(em: Emitter, frames, kin: Kin, link: str, p, prefix: str):
+    """Centre of a sphere at offset p of `link`: t + R p, evaluated as t, then one fused
+    multiply-add per column of R, for every coordinate.  The frame's entries are used as they
+    are (constants are not folded into the chain), so a centre computed from frame values held in
+    registers, in local memory or on the CPU rounds identically."""
+    fid, v = kin.sphere_in_frame(link, p)
+    R, t = frames[fid]
+    out = []
+    for r in range(3):
+        acc = t[r]
+        for k in range(3):
+            acc = em.assign(em._fma(R[r][k], em.const(float(v[k])), acc))
+        last = em.lines[-1]
+        name = f"{prefix}{'xyz'[r]}"
+        em.lines[-1] = last.replace(f"const {em.ty} {acc} =", f"const {em.ty} {name} =", 1)
+        out.append(name)
+    return out
+
+
+# sin_ref + cos_ref of one joint angle: 24 + 25 floating-point operations (vg_check.cuh)
+SINCOS_FLOPS = 49
+# one sphere centre from its frame: 9 fused multiply-adds
+CENTRE_FLOPS = 18
+
+
+def fk_flops(model: dict) -> dict:
+    """Floating-point operations of the generated FP32 kinematics for one configuration."""
+    kin = Kin(model)
+    em = Emitter("cuda", 1e-9)
+    emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
+    n_rev = sum(1 for f in kin.frames if f["type"] in ("revolute", "continuous"))
+    slots, _ = slot_table(model)
+    return {"frames": em.flops + SINCOS_FLOPS * n_rev, "centre": CENTRE_FLOPS, "slots": len(slots)}
+
+
+def frame_values(kin: Kin, frames) -> list:
+    """Every frame (root first, then movable frames in order) as 12 values: R row-major, t."""
+    out = []
+    for fid in ["root"] + [f["id"] for f in kin.frames]:
+        R, t = frames[fid]
+        out.append([R[r][c] for r in range(3) for c in range(3)] + list(t))
+    return out
+
+
+def frame_index(kin: Kin) -> dict:
+    return {fid: i for i, fid in enumerate(["root"] + [f["id"] for f in kin.frames])}
+
+
+def struct_name(name: str) -> str:
+    return name[0].upper() + name[1:]
+
+
+def slot_table(model: dict):
+    """Slot order: fine spheres 0..n-1 (reference order), then one coarse sphere per env link."""
+    slots = [(f["link"], f["p"], f["r"]) for f in model["fine_spheres"]]
+    coarse_slot = {}
+    for e in model["env_checks"]:
+        link = e["link"]
+        c = model["coarse_spheres"][link]
+        coarse_slot[link] = len(slots)
+        slots.append((link, c["p"], c["r"]))
+    return slots, coarse_slot
+
+
+# --------------------------------------------------------------------------------------------
+# CUDA output
+
+
+# Robots whose check schedule is emitted as table-driven loops (frames in local memory) rather
+# than straight-line code: their schedules are large enough (hundreds of link pairs) that
+# straight-line code spends minutes in ptxas and spills heavily.  Results are identical either way.
+TABLED = {"fetch", "baxter"}
+
+
+def _pairs_ab(e):
+    A, B = [], []
+    for sa, sb in e["fine"]:
+        if sa not in A:
+            A.append(sa)
+        if sb not in B:
+            B.append(sb)
+    # the reference's fine pairs for a link pair are the cross product of the two links' spheres
+    assert [[x, y] for x in A for y in B] == e["fine"], "fine self pairs are not a cross product"
+    return A, B
+
+
+def gen_cuda(model: dict) -> str:
+    name = model["name"]
+    S = struct_name(name)
+    kin = Kin(model)
+    slots, coarse_slot = slot_table(model)
+    dim = model["dimension"]
+    tabled = name in TABLED
+    fidx = frame_index(kin)
+    lines = []
+    w = lines.append
+    w("// Generated by vamp_gb300/robotgen/codegen.py from vamp_gb300/robots/%s.json. Do not edit." % name)
+    w("//")
+    w("// FP32 forward kinematics and the fkcc check schedule of the %s robot, one configuration" % name)
+    w("// per thread.  Schedule order follows the reference's generated Robot::fkcc")
+    w("// (src/impl/vamp/robots/%s.hh): environment checks link by link, each a coarse link sphere" % name)
+    w("// gating that link's fine spheres, then self-collision link pairs, a coarse pair gating the")
+    w("// cross product of the two links' fine spheres.  Schedule form: %s." % ("table-driven loops" if tabled else "straight-line"))
+    w("#pragma once")
+    w("")
+    w('#include "../vg_check.cuh"')
+    w("")
+    w("namespace vg::robots")
+    w("{")
+
+    def frames_block(em):
+        return emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: f"float {s_}, {c}; vg_sincos_ref({x}, &{s_}, &{c});")
+
+    # ---- tables (constant memory) for the table-driven form, and slot data for both
+    env_start, env_fine = [0], []
+    for e in model["env_checks"]:
+        env_fine += e["fine"]
+        env_start.append(len(env_fine))
+    self_rows, self_list = [], []
+    for e in model["self_checks"]:
+        A, B = _pairs_ab(e)
+        a0 = len(self_list)
+        self_list += A
+        b0 = len(self_list)
+        self_list += B
+        self_rows.append((coarse_slot[e["links"][0]], coarse_slot[e["links"][1]], a0, b0, len(A), len(B)))
+    if tabled:
+        pre = f"k{S}"
+        w(f"    // slot -> frame, and the slot's centre offset in that frame and radius")
+        w(f"    __constant__ int {pre}SlotFrame[{len(slots)}] = {{{', '.join(str(fidx[kin.sphere_in_frame(l, p)[0]]) for l, p, r in slots)}}};")
+        offs = []
+        em0 = Emitter("cuda", 1e-9)
+        for l, p, r in slots:
+            v = kin.sphere_in_frame(l, p)[1]
+            offs.append(f"{{{lit32(em0.const(float(v[0])))}, {lit32(em0.const(float(v[1])))}, {lit32(em0.const(float(v[2])))}, {lit32(r)}}}")
+        w(f"    __constant__ float4 {pre}SlotOff[{len(slots)}] = {{{', '.join(offs)}}};")
+        w(f"    __constant__ int {pre}EnvCoarse[{len(model['env_checks'])}] = {{{', '.join(str(coarse_slot[e['link']]) for e in model['env_checks'])}}};")
+        w(f"    __constant__ int {pre}EnvStart[{len(env_start)}] = {{{', '.join(map(str, env_start))}}};")
+        w(f"    __constant__ int {pre}EnvFine[{len(env_fine)}] = {{{', '.join(map(str, env_fine))}}};")
+        w(f"    // per link pair: coarse slot A, coarse slot B, start of A's and B's fine lists, their sizes")
+        w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
+        w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
+        w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
+        w("")
+
+    w("struct %s" % S)
+    w("{")
+    w("    static constexpr const char *kName = \"%s\";" % name)
+    w("    static constexpr int kDim = %d;" % dim)
+    w("    static constexpr int kFine = %d;" % len(model["fine_spheres"]))
+    w("    static constexpr int kSlots = %d;" % len(slots))
+    w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
+    w("    static constexpr int kResolution = %d;" % model["resolution"])
+    w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
+    w("    static constexpr float kMaxRadius = %s;" % lit32(model["max_radius"]))
+    w("    static constexpr float kScaleM[%d] = {%s};" % (dim, ", ".join(lit32(v) for v in model["s_m"])))
+    w("    static constexpr float kScaleA[%d] = {%s};" % (dim, ", ".join(lit32(v) for v in model["s_a"])))
+    w("")
+
+    # ---- all sphere slots, straight-line (FK queries)
+    em = Emitter("cuda", 1e-9)
+    fr = frames_block(em)
+    body = list(em.lines)
+    for i, (link, p, r) in enumerate(slots):
+        em.lines = []
+        x, y, z = emit_centre(em, fr, kin, link, p, f"s{i}_")
+        body += em.lines
+        body.append(f"out[{4 * i}] = {x}; out[{4 * i + 1}] = {y}; out[{4 * i + 2}] = {z}; out[{4 * i + 3}] = {lit32(r)};")
+    w("    // Every sphere slot: fine spheres 0..kFine-1, then the coarse sphere of each checked link.")
+    w("    static __device__ __forceinline__ void spheres(const float *q, float *out)")
+    w("    {")
+    for l in body:
+        w("        " + l)
+    w("    }")
+    w("")
+
+    if tabled:
+        em = Emitter("cuda", 1e-9)
+        fr = frames_block(em)
+        body = list(em.lines)
+        for i, vals in enumerate(frame_values(kin, fr)):
+            body.append(" ".join(f"F[{12 * i + j}] = {em.ref(v)};" for j, v in enumerate(vals)))
+        w("    // Frames (root first): R row-major then t, 12 floats each.")
+        w("    static __device__ __forceinline__ void frames(const float *q, float *F)")
+        w("    {")
+        for l in body:
+            w("        " + l)
+        w("    }")
+        w("")
+        pre = f"k{S}"
+        w(f"""    static __device__ __forceinline__ float4 centre(const float *F, int slot)
+    {{
+        const float *f = F + 12 * {pre}SlotFrame[slot];
+        const float4 o = {pre}SlotOff[slot];
+        float c[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {{
+            float acc = f[9 + r];
+            acc = __fmaf_rn(f[3 * r + 0], o.x, acc);
+            acc = __fmaf_rn(f[3 * r + 1], o.y, acc);
+            acc = __fmaf_rn(f[3 * r + 2], o.z, acc);
+            c[r] = acc;
+        }}
+        return make_float4(c[0], c[1], c[2], o.w);
+    }}
+
+    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.
+    template <typename Ctx>
+    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)
+    {{
+        float F[kFrames * 12];
+        frames(q, F);
+#pragma unroll 1
+        for (int c = 0; c < {len(model['env_checks'])}; ++c)
+        {{
+            const float4 k = centre(F, {pre}EnvCoarse[c]);
+            unsigned need = ctx.env_hit(k.x, k.y, k.z, k.w, ctx.alive);
+#pragma unroll 1
+            for (int i = {pre}EnvStart[c]; need && i < {pre}EnvStart[c + 1]; ++i)
+            {{
+                const float4 s = centre(F, {pre}EnvFine[i]);
+                const unsigned hit = ctx.env_hit(s.x, s.y, s.z, s.w, need);
+                need &= ~hit;
+                if (hit && !(ctx.alive &= ~hit))
+                {{
+                    return;
+                }}
+            }}
+        }}
+#pragma unroll 1
+        for (int c = 0; c < {len(self_rows)}; ++c)
+        {{
+            const int4 row = {pre}SelfRow[c];
+            const float4 a = centre(F, row.x), b = centre(F, row.y);
+            unsigned need = ctx.self_hit(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, ctx.alive);
+            if (!need)
+            {{
+                continue;
+            }}
+            const int2 len = {pre}SelfLen[c];
+#pragma unroll 1
+            for (int i = 0; need && i < len.x; ++i)
+            {{
+                const float4 sa = centre(F, {pre}SelfList[row.z + i]);
+#pragma unroll 1
+                for (int j = 0; need && j < len.y; ++j)
+                {{
+                    const float4 sb = centre(F, {pre}SelfList[row.w + j]);
+                    const unsigned hit = ctx.self_hit(sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w, need);
+                    need &= ~hit;
+                    if (hit && !(ctx.alive &= ~hit))
+                    {{
+                        return;
+                    }}
+                }}
+            }}
+        }}
+    }}""")
+        w("};")
+        w("}  // namespace vg::robots")
+        return "\n".join(lines) + "\n"
+
+    # ---- straight-line schedule
+    em = Emitter("cuda", 1e-9)
+    fr = frames_block(em)
+    body = list(em.lines)
+    max_a = max([len(e["fine"]) for e in model["env_checks"]] + [len(_pairs_ab(e)[0]) for e in model["self_checks"]])
+    max_b = max([1] + [len(_pairs_ab(e)[1]) for e in model["self_checks"]])
+    body.append(f"float4 sa[{max_a}], sb[{max_b}];  // fine sphere scratch, reused by every check")
+
+    def centre(i, tag):
+        em.lines = []
+        link, p, r = slots[i]
+        x, y, z = emit_centre(em, fr, kin, link, p, f"{tag}{i}_")
+        return list(em.lines), (x, y, z, lit32(r))
+
+    # One __noinline__ function per distinct ordered list of fine spheres, taking the symbolic
+    # entries of the link's frame and writing centres and radii.
+    fine_fns = {}
+    fine_defs = []
+
+    def fine_call(lst):
+        key = tuple(lst)
+        fid = kin.sphere_in_frame(slots[lst[0]][0], slots[lst[0]][1])[0]
+        for sidx in lst:
+            assert kin.sphere_in_frame(slots[sidx][0], slots[sidx][1])[0] == fid
+        R, t = fr[fid]
+        params = [v for row in R for v in row] + list(t)
+        params = [v for v in params if isinstance(v, str)]
+        params = [v[1:] if v.startswith("-") else v for v in params]
+        params = list(dict.fromkeys(params))
+        if key not in fine_fns:
+            fn = f"fine_{len(fine_fns)}"
+            fine_fns[key] = fn
+            fe = Emitter("cuda", 1e-9)
+            fe.n = 100000
+            flines = []
+            for k, sidx in enumerate(lst):
+                fe.lines = []
+                link, p, r = slots[sidx]
+                x, y, z = emit_centre(fe, fr, kin, link, p, f"s{k}_")
+                flines += fe.lines
+                flines.append(f"out[{k}] = make_float4({x}, {y}, {z}, {lit32(r)});")
+            sig = ", ".join([f"const float {v}" for v in params] + ["float4 *out"])
+            fine_defs.append(f"    // fine spheres {list(lst)} ({slots[lst[0]][0]})")
+            fine_defs.append(f"    static __device__ __noinline__ void {fn}({sig})")
+            fine_defs.append("    {")
+            fine_defs.extend("        " + l for l in flines)
+            fine_defs.append("    }")
+        return f"{fine_fns[key]}({', '.join(params + [''])}"
+
+    for e in model["env_checks"]:
+        link = e["link"]
+        ls, (x, y, z, r) = centre(coarse_slot[link], "c")
+        body.append(f"// environment: {link}")
+        body.append("{")
+        body += ["    " + l for l in ls]
+        body.append(f"    const unsigned need = ctx.env_hit({x}, {y}, {z}, {r}, ctx.alive);")
+        body.append("    if (need)")
+        body.append("    {")
+        body.append(f"        {fine_call(e['fine'])}sa);")
+        body.append(f"        if (vg::env_fine<{len(e['fine'])}>(ctx, sa, need)) return;")
+        body.append("    }")
+        body.append("}")
+    for e in model["self_checks"]:
+        a, b = e["links"]
+        la, (ax, ay, az, ar) = centre(coarse_slot[a], "ca")
+        lb, (bx, by, bz, br) = centre(coarse_slot[b], "cb")
+        A, B = _pairs_ab(e)
+        body.append(f"// self: {a} vs. {b}")
+        body.append("{")
+        body += ["    " + l for l in la + lb]
+        body.append(f"    const unsigned need = ctx.self_hit({ax}, {ay}, {az}, {ar}, {bx}, {by}, {bz}, {br}, ctx.alive);")
+        body.append("    if (need)")
+        body.append("    {")
+        body.append(f"        {fine_call(A)}sa);")
+        body.append(f"        {fine_call(B)}sb);")
+        body.append(f"        if (vg::self_cross<{len(A)}, {len(B)}>(ctx, sa, sb, need)) return;")
+        body.append("    }")
+        body.append("}")
+
+    for l in fine_defs:
+        w(l)
+    w("")
+    w("    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.")
+    w("    template <typename Ctx>")
+    w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
+    w("    {")
+    for l in body:
+        w("        " + l)
+    w("    }")
+    w("};")
+    w("}  // namespace vg::robots")
+    return "\n".join(lines) + "\n"
+
+
+# --------------------------------------------------------------------------------------------
+# C oracle output
+
+
+def gen_c(model: dict) -> str:
+    name = model["name"]
+    kin = Kin(model)
+    slots, coarse_slot = slot_table(model)
+    dim = model["dimension"]
+    P = name.upper()
+    lines = []
+    w = lines.append
+    w("/* Generated by vamp_gb300/robotgen/codegen.py from vamp_gb300/robots/%s.json. Do not edit." % name)
+    w(" *")
+    w(" * CPU oracle tables and kinematics for the %s robot.  Test infrastructure only." % name)
+    w(" * Schedule: the reference's Robot::fkcc (src/impl/vamp/robots/%s.hh), as tables." % name)
+    w(" * FK: the same FP32 operation sequence as the CUDA kernels, plus an FP64 version. */")
+    w("#pragma once")
+    w("#include <math.h>")
+    w('#include "../vgo_math.h"')
+    w("")
+    w("#define VGO_%s_DIM %d" % (P, dim))
+    w("#define VGO_%s_FINE %d" % (P, len(model["fine_spheres"])))
+    w("#define VGO_%s_SLOTS %d" % (P, len(slots)))
+    w("#define VGO_%s_RESOLUTION %d" % (P, model["resolution"]))
+    w("static const float vgo_%s_s_m[%d] = {%s};" % (name, dim, ", ".join(lit32(v) for v in model["s_m"])))
+    w("static const float vgo_%s_s_a[%d] = {%s};" % (name, dim, ", ".join(lit32(v) for v in model["s_a"])))
+    w("static const float vgo_%s_radius_range[2] = {%s, %s};" % (name, lit32(model["min_radius"]), lit32(model["max_radius"])))
+    # env schedule
+    env_coarse = [coarse_slot[e["link"]] for e in model["env_checks"]]
+    env_start, env_fine = [], []
+    for e in model["env_checks"]:
+        env_start.append(len(env_fine))
+        env_fine += e["fine"]
+    env_start.append(len(env_fine))
+    w("#define VGO_%s_ENV_CHECKS %d" % (P, len(env_coarse)))
+    w("static const int vgo_%s_env_coarse[] = {%s};" % (name, ", ".join(map(str, env_coarse))))
+    w("static const int vgo_%s_env_start[] = {%s};" % (name, ", ".join(map(str, env_start))))
+    w("static const int vgo_%s_env_fine[] = {%s};" % (name, ", ".join(map(str, env_fine))))
+    self_coarse, self_start, self_fine = [], [], []
+    for e in model["self_checks"]:
+        a, b = e["links"]
+        self_coarse += [coarse_slot[a], coarse_slot[b]]
+        self_start.append(len(self_fine) // 2)
+        for sa, sb in e["fine"]:
+            self_fine += [sa, sb]
+    self_start.append(len(self_fine) // 2)
+    w("#define VGO_%s_SELF_CHECKS %d" % (P, len(model["self_checks"])))
+    w("static const int vgo_%s_self_coarse[] = {%s};" % (name, ", ".join(map(str, self_coarse)) or "0"))
+    w("static const int vgo_%s_self_start[] = {%s};" % (name, ", ".join(map(str, self_start))))
+    w("static const int vgo_%s_self_fine[] = {%s};" % (name, ", ".join(map(str, self_fine)) or "0"))
+    w("")
+
+    for tgt, ty, sc in (("c32", "float", "vgo_sincos_ref"), ("c64", "double", None)):
+        em = Emitter(tgt, 1e-9 if tgt == "c32" else 0.0)
+        if tgt == "c32":
+            scf = lambda x, s, c: f"float {s}, {c}; vgo_sincos_ref({x}, &{s}, &{c});"
+        else:
+            scf = lambda x, s, c: f"const double {s} = sin({x}), {c} = cos({x});"
+        fr = emit_frames(kin, em, "q", sc_fn=scf)
+        body = list(em.lines)
+        for i, (link, p, r) in enumerate(slots):
+            em.lines = []
+            x, y, z = emit_centre(em, fr, kin, link, p, f"s{i}_")
+            body += em.lines
+            rr = lit32(r) if tgt == "c32" else lit64(f32(r))
+            body.append(f"out[{4 * i}] = {em.ref(x)}; out[{4 * i + 1}] = {em.ref(y)}; out[{4 * i + 2}] = {em.ref(z)}; out[{4 * i + 3}] = {rr};")
+        suffix = "f32" if tgt == "c32" else "f64"
+        w(f"/* Every sphere slot (fine, then coarse), {ty}: out[4 * slot + (x, y, z, r)]. */")
+        w(f"static void vgo_{name}_spheres_{suffix}(const {ty} *q, {ty} *out)")
+        w("{")
+        for l in body:
+            w("    " + l)
+        w("}")
+        w("")
+    return "\n".join(lines) + "\n"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("robots", nargs="*", default=["panda", "ur5", "fetch", "baxter"])
+    a = ap.parse_args()
+    CUDA_OUT.mkdir(parents=True, exist_ok=True)
+    C_OUT.mkdir(parents=True, exist_ok=True)
+    for r in a.robots:
+        model = json.loads((MODELS / f"{r}.json").read_text())
+        (CUDA_OUT / f"{r}.cuh").write_text(gen_cuda(model))
+        (C_OUT / f"{r}.h").write_text(gen_c(model))
+        print(r, "ok")
+
+
+if __name__ == "__main__":
+    main()
