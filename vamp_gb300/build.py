@@ -44,9 +44,15 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
+def _defines() -> list[str]:
+    # VG_MIN_BLOCKS: resident 128-thread blocks per SM the kernels are compiled for
+    mb = os.environ.get("VG_MIN_BLOCKS")
+    return [f"-DVG_MIN_BLOCKS={int(mb)}"] if mb else []
+
+
 def _compile(src: Path, verbose: bool) -> tuple[Path, str]:
     obj = BUILD / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_defines(), "-c", str(src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,6 +74,11 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
     BUILD.mkdir(exist_ok=True)
     srcs = sources()
+    stamp = BUILD / "defines.txt"
+    defs = " ".join(_defines())
+    if not stamp.exists() or stamp.read_text() != defs:
+        force = True
+        stamp.write_text(defs)
     todo = [s for s in srcs if force or _stale(BUILD / (s.stem + ".o"), s)]
     logs = {}
     if todo:

@@ -240,85 +240,177 @@ namespace vg
         return __fadd_rn(__fsqrt_rn(v), r);
     }
 
-    // One kind's primitive loop for the segments in `scan`; returns the lanes whose segment hit.
-    template <int W, int KIND>
-    __device__ __forceinline__ unsigned kind_loop(
-        const EnvView &e, unsigned scan, float me, float x, float y, float z, float rr)
+    // max over the W lanes of a segment (segments are aligned groups of W lanes)
+    template <int W>
+    __device__ __forceinline__ float seg_max(float v)
     {
-        unsigned hit = 0;
+#pragma unroll
+        for (int o = 1; o < W; o <<= 1)
+        {
+            v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+        }
+        return v;
+    }
+
+    __device__ __forceinline__ float warp_max(float v)
+    {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+        }
+        return v;
+    }
+
+    template <int KIND>
+    __device__ __forceinline__ float prim_test(const float4 *o, float x, float y, float z, float r, float rsq)
+    {
+        if constexpr (KIND == 0)
+            return t_sphere(o, x, y, z, r);
+        else if constexpr (KIND == 1)
+            return t_capsule(o, x, y, z, r);
+        else if constexpr (KIND == 2)
+            return t_zcapsule(o, x, y, z, r);
+        else if constexpr (KIND == 3)
+            return t_cuboid(o, x, y, z, rsq);
+        else
+            return t_zcuboid(o, x, y, z, rsq);
+    }
+
+    // One kind's sorted primitive list against NS query spheres.
+    //
+    // The reference walks the list per sphere and stops at the first object whose min_distance
+    // minus max_extent has a clear sign bit in every lane of the block.  Since min_distance is
+    // sorted and rounding is monotone, that stop is the first object with min_distance >= M, M
+    // being the largest max_extent over the block's lanes; the objects before it are tested and a
+    // collision is any lane's test with its sign bit set.  Here each object record is read once
+    // for the NS spheres; sphere s tests it while min_distance < Mw[s] (the warp's largest M for
+    // that sphere, a uniform branch) and counts the result only while min_distance < M[s] (its
+    // own segment's bound).  Sign bits are OR-ed into bits[]; the segment vote happens once.
+    template <int KIND, int NS>
+    __device__ __forceinline__ void kind_pass(
+        const EnvView &e, float Mall, const float *Mw, const float *M, const float *x, const float *y,
+        const float *z, const float *r, const float *rsq, unsigned *bits)
+    {
         const float4 *rec = e.rec[KIND];
         const int n = e.n[KIND];
+#pragma unroll 1
         for (int i = 0; i < n; ++i)
         {
             const float4 *o = rec + i * rec_f4(KIND);
             const float md = reinterpret_cast<const float *>(o)[min_d_offset(KIND)];
-            // the segment stops at this object when every lane's (min_d - max_extent) has a
-            // clear sign bit
-            const unsigned stop = seg_all<W>(__ballot_sync(kFull, !signbit_set(__fsub_rn(md, me))));
-            scan &= ~stop;
-            if (!scan)
+            if (!(md < Mall))
             {
                 break;
             }
-            float t;
-            if constexpr (KIND == 0)
-                t = t_sphere(o, x, y, z, rr);
-            else if constexpr (KIND == 1)
-                t = t_capsule(o, x, y, z, rr);
-            else if constexpr (KIND == 2)
-                t = t_zcapsule(o, x, y, z, rr);
-            else if constexpr (KIND == 3)
-                t = t_cuboid(o, x, y, z, rr);
-            else
-                t = t_zcuboid(o, x, y, z, rr);
-            const unsigned h = seg_any<W>(__ballot_sync(kFull, signbit_set(t))) & scan;
-            hit |= h;
-            scan &= ~h;
-            if (!scan)
+#pragma unroll
+            for (int s = 0; s < NS; ++s)
             {
-                break;
+                if (md < Mw[s])
+                {
+                    const float t = prim_test<KIND>(o, x[s], y[s], z[s], r[s], rsq[s]);
+                    bits[s] |= md < M[s] ? __float_as_uint(t) : 0u;
+                }
             }
         }
+    }
+
+    // sphere_environment_in_collision (validity.hh:47-150) for NS spheres at once, each over the
+    // segments in `mask`.  hit[s] receives the lanes of the segments whose block collides for
+    // sphere s.  Warp-uniform; all 32 lanes must call.
+    template <int W, int NS>
+    __device__ __forceinline__ void env_multi(const EnvView &e, const float4 *sph, unsigned mask, unsigned *hit)
+    {
+        const int lane = threadIdx.x & 31;
+        const bool on = (mask >> lane) & 1u;
+        float x[NS], y[NS], z[NS], r[NS], rsq[NS], M[NS], Mw[NS];
+        unsigned bits[NS];
+        float Mall = -__int_as_float(0x7f800000);
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+        {
+            const float4 c = sph[s];
+            x[s] = c.x;
+            y[s] = c.y;
+            z[s] = c.z;
+            r[s] = c.w;
+            rsq[s] = __fmul_rn(c.w, c.w);
+            const float v = __fmaf_rn(c.x, c.x, __fmaf_rn(c.z, c.z, __fmul_rn(c.y, c.y)));
+            const float m = seg_max<W>(max_extent(e, v, c.w));
+            M[s] = on ? m : -__int_as_float(0x7f800000);
+            Mw[s] = warp_max(M[s]);
+            Mall = fmaxf(Mall, Mw[s]);
+            bits[s] = 0u;
+        }
+        kind_pass<0, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+        kind_pass<1, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+        kind_pass<2, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+        kind_pass<3, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+        kind_pass<4, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+        {
+            hit[s] = seg_any<W>(__ballot_sync(kFull, bits[s] >> 31)) & mask;
+        }
+    }
+
+    // A frame as 12 floats: R row-major, then t.
+    struct Frame
+    {
+        float m[12];
+    };
+
+    // t + R o for a point offset o (o.w, the radius, is passed through): t, then one fused
+    // multiply-add per column of R, for every coordinate (the generated kinematics' order).
+    __device__ __forceinline__ float4 frame_point(const Frame &f, const float4 o)
+    {
+        float c[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+            float acc = f.m[9 + r];
+            acc = __fmaf_rn(f.m[3 * r + 0], o.x, acc);
+            acc = __fmaf_rn(f.m[3 * r + 1], o.y, acc);
+            acc = __fmaf_rn(f.m[3 * r + 2], o.z, acc);
+            c[r] = acc;
+        }
+        return make_float4(c[0], c[1], c[2], o.w);
+    }
+
+    // Single-sphere query, inlined into the caller.
+    template <int W>
+    __device__ __forceinline__ unsigned env_query_inline(const EnvView &e, float x, float y, float z, float r, unsigned mask)
+    {
+        const float4 s = make_float4(x, y, z, r);
+        unsigned hit;
+        env_multi<W, 1>(e, &s, mask, &hit);
         return hit;
     }
 
-    // sphere_environment_in_collision (validity.hh:47-150) for the segments in `mask`: returns
-    // the lanes of the segments whose block collides.  Warp-uniform; all 32 lanes must call.
+    // Single-sphere form.
     template <int W>
     __device__ __noinline__ unsigned env_query(const EnvView &e, float x, float y, float z, float r, unsigned mask)
     {
-        const float v = __fmaf_rn(x, x, __fmaf_rn(z, z, __fmul_rn(y, y)));
-        const float me = max_extent(e, v, r);
-        const float rsq = __fmul_rn(r, r);
-        unsigned hit = 0;
-        unsigned todo = mask;
-        unsigned h = kind_loop<W, 0>(e, todo, me, x, y, z, r);
-        hit |= h;
-        todo &= ~h;
-        if (todo)
-        {
-            h = kind_loop<W, 1>(e, todo, me, x, y, z, r);
-            hit |= h;
-            todo &= ~h;
-        }
-        if (todo)
-        {
-            h = kind_loop<W, 2>(e, todo, me, x, y, z, r);
-            hit |= h;
-            todo &= ~h;
-        }
-        if (todo)
-        {
-            h = kind_loop<W, 3>(e, todo, me, x, y, z, rsq);
-            hit |= h;
-            todo &= ~h;
-        }
-        if (todo)
-        {
-            h = kind_loop<W, 4>(e, todo, me, x, y, z, rsq);
-            hit |= h;
-        }
+        const float4 s = make_float4(x, y, z, r);
+        unsigned hit;
+        env_multi<W, 1>(e, &s, mask, &hit);
         return hit;
+    }
+
+    // Fine tests of one link's NS spheres (one function per distinct NS): the segments in `mask`
+    // whose block collides for any of the spheres.
+    template <int W, int NS>
+    __device__ __noinline__ unsigned env_any(const EnvView &e, const float4 *sph, unsigned mask)
+    {
+        unsigned hit[NS];
+        env_multi<W, NS>(e, sph, mask, hit);
+        unsigned any = 0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+        {
+            any |= hit[s];
+        }
+        return any;
     }
 
     // sphere_sphere_self_collision (validity.hh:23-44) for the segments in `mask`.
@@ -331,16 +423,38 @@ namespace vg
         return seg_any<W>(__ballot_sync(kFull, signbit_set(t))) & mask;
     }
 
+    // Sign bit of one fine self-collision test, for OR-accumulation; rs is the pair's radius sum.
+    __device__ __forceinline__ unsigned self_bits(float ax, float ay, float az, float bx, float by, float bz, float rs)
+    {
+        return __float_as_uint(__fmaf_rn(-rs, rs, sql2(ax, ay, az, bx, by, bz)));
+    }
+
     // The context a generated Robot::fkcc body runs against.
     template <int W>
     struct CheckCtx
     {
+        static constexpr int kW = W;
         const EnvView &env;
         unsigned alive;
+        // every active lane's configuration lies inside the joint limits widened by the culling
+        // slack: fine self pairs proven unable to collide there may be skipped
+        bool in_limits = false;
 
         __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
         {
             return env_query<W>(env, x, y, z, r, mask);
+        }
+
+        template <int NS>
+        __device__ __forceinline__ void env_many(const float4 *s, unsigned mask, unsigned *hit)
+        {
+            env_multi<W, NS>(env, s, mask, hit);
+        }
+
+        template <int NS>
+        __device__ __forceinline__ unsigned env_any_hit(const float4 *s, unsigned mask)
+        {
+            return env_any<W, NS>(env, s, mask);
         }
 
         __device__ __forceinline__ unsigned self_hit(
@@ -348,7 +462,14 @@ namespace vg
         {
             return self_query<W>(ax, ay, az, ar, bx, by, bz, br, mask);
         }
+
+        // the segments in `mask` for which any OR-accumulated sign bit is set
+        __device__ __forceinline__ unsigned vote(unsigned bits, unsigned mask)
+        {
+            return seg_any<W>(__ballot_sync(kFull, bits >> 31)) & mask;
+        }
     };
+
     // Fine environment tests of one link's spheres, in order, for the segments in `need`.
     // Clears colliding segments from ctx.alive; returns true once none is left.
     template <int N, typename Ctx>

@@ -14,6 +14,11 @@
 
 #include "vg_check.cuh"
 
+// Resident blocks of 128 threads per SM the kernels are compiled for (caps their registers).
+#ifndef VG_MIN_BLOCKS
+#define VG_MIN_BLOCKS 1
+#endif
+
 namespace vg
 {
     // Device image of an environment: the x86 RSQRTPS table followed by the primitive records
@@ -66,7 +71,7 @@ namespace vg
     };
 
     template <typename Robot>
-    __global__ void __launch_bounds__(128) states_kernel(StatesParams p)
+    __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) states_kernel(StatesParams p)
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
@@ -130,7 +135,7 @@ namespace vg
     }
 
     template <typename Robot, int W>
-    __global__ void __launch_bounds__(128) edges_kernel(EdgesParams p)
+    __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);

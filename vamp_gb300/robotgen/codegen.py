@@ -333,7 +333,7 @@ CENTRE_FLOPS = 18
 def fk_flops(model: dict) -> dict:
     """Floating-point operations of the generated FP32 kinematics for one configuration."""
     kin = Kin(model)
-    em = Emitter("cuda", 1e-9)
+    em = Emitter("cuda", SNAP32)
     emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
     n_rev = sum(1 for f in kin.frames if f["type"] in ("revolute", "continuous"))
     slots, _ = slot_table(model)
@@ -376,7 +376,35 @@ def slot_table(model: dict):
 # Robots whose check schedule is emitted as table-driven loops (frames in local memory) rather
 # than straight-line code: their schedules are large enough (hundreds of link pairs) that
 # straight-line code spends minutes in ptxas and spills heavily.  Results are identical either way.
-TABLED = {"fetch", "baxter"}
+TABLED = {"ur5", "fetch", "baxter"}
+# FP32 constants this close to 0 or +-1 are folded to exact values: URDF angles such as
+# 1.570796325 leave ~1e-9 residues that only cost operations (their effect is below 1e-8 m)
+SNAP32 = 1e-7
+# coarse environment queries evaluated together in one pass over the objects
+COARSE_BATCH = 6
+
+
+def load_cull(name: str):
+    """Live fine self pairs per self check (None: all live), from robots/<name>.cull.json."""
+    path = MODELS / f"{name}.cull.json"
+    if not path.exists():
+        return None
+    return json.loads(path.read_text())
+
+
+def limits_code(model: dict, cull) -> list:
+    """Lines setting ctx.in_limits: every active lane's configuration lies in the joint limits
+    widened by the culling slack (the precondition for skipping culled self pairs)."""
+    if cull is None:
+        return ["ctx.in_limits = false;"]
+    slack = cull["slack_rad"]
+    lines = ["bool inl = true;"]
+    for d, (m_, a_) in enumerate(zip(model["s_m"], model["s_a"])):
+        lo = f32(a_ - slack)
+        hi = f32(a_ + m_ + slack)
+        lines.append(f"inl &= (q[{d}] >= {lit32(lo)}) & (q[{d}] <= {lit32(hi)});")
+    lines.append("ctx.in_limits = __all_sync(vg::kFull, inl || !((ctx.alive >> (threadIdx.x & 31)) & 1u));")
+    return lines
 
 
 def _pairs_ab(e):
@@ -431,12 +459,12 @@ def gen_cuda(model: dict) -> str:
         b0 = len(self_list)
         self_list += B
         self_rows.append((coarse_slot[e["links"][0]], coarse_slot[e["links"][1]], a0, b0, len(A), len(B)))
-    if tabled:
+    if True:
         pre = f"k{S}"
         w(f"    // slot -> frame, and the slot's centre offset in that frame and radius")
         w(f"    __constant__ int {pre}SlotFrame[{len(slots)}] = {{{', '.join(str(fidx[kin.sphere_in_frame(l, p)[0]]) for l, p, r in slots)}}};")
         offs = []
-        em0 = Emitter("cuda", 1e-9)
+        em0 = Emitter("cuda", SNAP32)
         for l, p, r in slots:
             v = kin.sphere_in_frame(l, p)[1]
             offs.append(f"{{{lit32(em0.const(float(v[0])))}, {lit32(em0.const(float(v[1])))}, {lit32(em0.const(float(v[2])))}, {lit32(r)}}}")
@@ -448,6 +476,17 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
         w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
         w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
+        cull = load_cull(name)
+        live_start, live_pairs = [0], []
+        for ci, e in enumerate(model["self_checks"]):
+            sel = range(len(e["fine"])) if cull is None or cull["live"][ci] is None else cull["live"][ci]
+            live_pairs += [tuple(e["fine"][pi]) for pi in sel]
+            live_start.append(len(live_pairs))
+        w(f"    // fine pairs that can collide inside the widened joint limits, per self check")
+        w(f"    __constant__ int {pre}LiveStart[{len(live_start)}] = {{{', '.join(map(str, live_start))}}};")
+        w(f"    __constant__ int2 {pre}LivePair[{max(1, len(live_pairs))}] = {{{', '.join('{%d, %d}' % p for p in live_pairs) or '{0, 0}'}}};")
+        all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
+        w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         w("")
 
     w("struct %s" % S)
@@ -465,7 +504,7 @@ def gen_cuda(model: dict) -> str:
     w("")
 
     # ---- all sphere slots, straight-line (FK queries)
-    em = Emitter("cuda", 1e-9)
+    em = Emitter("cuda", SNAP32)
     fr = frames_block(em)
     body = list(em.lines)
     for i, (link, p, r) in enumerate(slots):
@@ -482,7 +521,7 @@ def gen_cuda(model: dict) -> str:
     w("")
 
     if tabled:
-        em = Emitter("cuda", 1e-9)
+        em = Emitter("cuda", SNAP32)
         fr = frames_block(em)
         body = list(em.lines)
         for i, vals in enumerate(frame_values(kin, fr)):
@@ -518,6 +557,7 @@ def gen_cuda(model: dict) -> str:
     {{
         float F[kFrames * 12];
         frames(q, F);
+{chr(10).join("        " + l for l in limits_code(model, load_cull(name)))}
 #pragma unroll 1
         for (int c = 0; c < {len(model['env_checks'])}; ++c)
         {{
@@ -545,22 +585,36 @@ def gen_cuda(model: dict) -> str:
             {{
                 continue;
             }}
-            const int2 len = {pre}SelfLen[c];
-#pragma unroll 1
-            for (int i = 0; need && i < len.x; ++i)
+            unsigned acc = 0u;
+            if (ctx.in_limits)
             {{
-                const float4 sa = centre(F, {pre}SelfList[row.z + i]);
 #pragma unroll 1
-                for (int j = 0; need && j < len.y; ++j)
+                for (int k = {pre}LiveStart[c]; k < {pre}LiveStart[c + 1]; ++k)
                 {{
-                    const float4 sb = centre(F, {pre}SelfList[row.w + j]);
-                    const unsigned hit = ctx.self_hit(sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w, need);
-                    need &= ~hit;
-                    if (hit && !(ctx.alive &= ~hit))
+                    const int2 pr = {pre}LivePair[k];
+                    const float4 sa = centre(F, pr.x), sb = centre(F, pr.y);
+                    acc |= vg::self_bits(sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, __fadd_rn(sa.w, sb.w));
+                }}
+            }}
+            else
+            {{
+                const int2 len = {pre}SelfLen[c];
+#pragma unroll 1
+                for (int i = 0; i < len.x; ++i)
+                {{
+                    const float4 sa = centre(F, {pre}SelfList[row.z + i]);
+#pragma unroll 1
+                    for (int j = 0; j < len.y; ++j)
                     {{
-                        return;
+                        const float4 sb = centre(F, {pre}SelfList[row.w + j]);
+                        acc |= vg::self_bits(sa.x, sa.y, sa.z, sb.x, sb.y, sb.z, __fadd_rn(sa.w, sb.w));
                     }}
                 }}
+            }}
+            const unsigned hit = ctx.vote(acc, need);
+            if (hit && !(ctx.alive &= ~hit))
+            {{
+                return;
             }}
         }}
     }}""")
@@ -568,13 +622,21 @@ def gen_cuda(model: dict) -> str:
         w("}  // namespace vg::robots")
         return "\n".join(lines) + "\n"
 
-    # ---- straight-line schedule
-    em = Emitter("cuda", 1e-9)
+    # ---- compact schedule: frames in registers, per-check code unrolled, per-sphere and per-pair
+    # work in rolled loops over constant tables (keeps the kernel small enough for the
+    # instruction cache)
+    pre = f"k{S}"
+    em = Emitter("cuda", SNAP32)
     fr = frames_block(em)
     body = list(em.lines)
-    max_a = max([len(e["fine"]) for e in model["env_checks"]] + [len(_pairs_ab(e)[0]) for e in model["self_checks"]])
-    max_b = max([1] + [len(_pairs_ab(e)[1]) for e in model["self_checks"]])
-    body.append(f"float4 sa[{max_a}], sb[{max_b}];  // fine sphere scratch, reused by every check")
+    body += limits_code(model, load_cull(name))
+    fvals = frame_values(kin, fr)
+
+    def frame_expr(fid):
+        return "vg::Frame{{" + ", ".join(em.ref(v) for v in fvals[fidx[fid]]) + "}}"
+
+    n_env = len(model["env_checks"])
+    env_index = {e["link"]: k for k, e in enumerate(model["env_checks"])}
 
     def centre(i, tag):
         em.lines = []
@@ -582,74 +644,105 @@ def gen_cuda(model: dict) -> str:
         x, y, z = emit_centre(em, fr, kin, link, p, f"{tag}{i}_")
         return list(em.lines), (x, y, z, lit32(r))
 
-    # One __noinline__ function per distinct ordered list of fine spheres, taking the symbolic
-    # entries of the link's frame and writing centres and radii.
-    fine_fns = {}
-    fine_defs = []
-
-    def fine_call(lst):
-        key = tuple(lst)
-        fid = kin.sphere_in_frame(slots[lst[0]][0], slots[lst[0]][1])[0]
-        for sidx in lst:
-            assert kin.sphere_in_frame(slots[sidx][0], slots[sidx][1])[0] == fid
-        R, t = fr[fid]
-        params = [v for row in R for v in row] + list(t)
-        params = [v for v in params if isinstance(v, str)]
-        params = [v[1:] if v.startswith("-") else v for v in params]
-        params = list(dict.fromkeys(params))
-        if key not in fine_fns:
-            fn = f"fine_{len(fine_fns)}"
-            fine_fns[key] = fn
-            fe = Emitter("cuda", 1e-9)
-            fe.n = 100000
-            flines = []
-            for k, sidx in enumerate(lst):
-                fe.lines = []
-                link, p, r = slots[sidx]
-                x, y, z = emit_centre(fe, fr, kin, link, p, f"s{k}_")
-                flines += fe.lines
-                flines.append(f"out[{k}] = make_float4({x}, {y}, {z}, {lit32(r)});")
-            sig = ", ".join([f"const float {v}" for v in params] + ["float4 *out"])
-            fine_defs.append(f"    // fine spheres {list(lst)} ({slots[lst[0]][0]})")
-            fine_defs.append(f"    static __device__ __noinline__ void {fn}({sig})")
-            fine_defs.append("    {")
-            fine_defs.extend("        " + l for l in flines)
-            fine_defs.append("    }")
-        return f"{fine_fns[key]}({', '.join(params + [''])}"
-
-    for e in model["env_checks"]:
-        link = e["link"]
-        ls, (x, y, z, r) = centre(coarse_slot[link], "c")
-        body.append(f"// environment: {link}")
+    # coarse spheres of every environment-checked link: queried together, reused by self checks
+    body.append(f"float4 cs[{n_env}];")
+    for k, e in enumerate(model["env_checks"]):
+        ls, (x, y, z, r) = centre(coarse_slot[e["link"]], "c")
         body.append("{")
         body += ["    " + l for l in ls]
-        body.append(f"    const unsigned need = ctx.env_hit({x}, {y}, {z}, {r}, ctx.alive);")
-        body.append("    if (need)")
+        body.append(f"    cs[{k}] = make_float4({x}, {y}, {z}, {r});  // {e['link']}")
+        body.append("}")
+    body.append(f"unsigned ch[{n_env}];")
+    nb = -(-n_env // COARSE_BATCH)
+    base = 0
+    for bi in range(nb):
+        size = n_env // nb + (1 if bi < n_env % nb else 0)
+        body.append(f"ctx.template env_many<{size}>(cs + {base}, ctx.alive, ch + {base});")
+        base += size
+    for k, e in enumerate(model["env_checks"]):
+        fid = kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0]
+        for sidx in e["fine"]:
+            assert kin.sphere_in_frame(slots[sidx][0], slots[sidx][1])[0] == fid
+        body.append(f"// environment: {e['link']} ({len(e['fine'])} fine spheres)")
+        body.append("{")
+        body.append(f"    const unsigned need = ch[{k}] & ctx.alive;")
+        body.append(f"    if (need)")
         body.append("    {")
-        body.append(f"        {fine_call(e['fine'])}sa);")
-        body.append(f"        if (vg::env_fine<{len(e['fine'])}>(ctx, sa, need)) return;")
+        body.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, {frame_expr(fid)}, {env_start[k]}, {env_start[k + 1]}, need);")
+        body.append("        if (hit && !(ctx.alive &= ~hit)) return;")
         body.append("    }")
         body.append("}")
-    for e in model["self_checks"]:
+    cull = load_cull(name)
+    full_start, full_pairs, lv_start, lv_pairs = [0], [], [0], []
+    for ci, e in enumerate(model["self_checks"]):
+        full_pairs += [tuple(p_) for p_ in e["fine"]]
+        full_start.append(len(full_pairs))
+        sel = range(len(e["fine"])) if cull is None or cull["live"][ci] is None else cull["live"][ci]
+        lv_pairs += [tuple(e["fine"][pi]) for pi in sel]
+        lv_start.append(len(lv_pairs))
+    for ci, e in enumerate(model["self_checks"]):
         a, b = e["links"]
-        la, (ax, ay, az, ar) = centre(coarse_slot[a], "ca")
-        lb, (bx, by, bz, br) = centre(coarse_slot[b], "cb")
         A, B = _pairs_ab(e)
-        body.append(f"// self: {a} vs. {b}")
+        fa = kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0]
+        fb = kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0]
+        ka, kb = env_index[a], env_index[b]
+        nl = lv_start[ci + 1] - lv_start[ci]
+        body.append(f"// self: {a} vs. {b} ({nl} of {len(e['fine'])} fine pairs can collide inside the limits)")
         body.append("{")
-        body += ["    " + l for l in la + lb]
-        body.append(f"    const unsigned need = ctx.self_hit({ax}, {ay}, {az}, {ar}, {bx}, {by}, {bz}, {br}, ctx.alive);")
+        body.append(f"    const unsigned need = ctx.self_hit(cs[{ka}].x, cs[{ka}].y, cs[{ka}].z, cs[{ka}].w, cs[{kb}].x, cs[{kb}].y, cs[{kb}].z, cs[{kb}].w, ctx.alive);")
         body.append("    if (need)")
         body.append("    {")
-        body.append(f"        {fine_call(A)}sa);")
-        body.append(f"        {fine_call(B)}sb);")
-        body.append(f"        if (vg::self_cross<{len(A)}, {len(B)}>(ctx, sa, sb, need)) return;")
+        body.append(f"        const unsigned acc = ctx.in_limits ? self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
+        body.append(f"                                           : self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
+        body.append("        const unsigned hit = ctx.vote(acc, need);")
+        body.append("        if (hit && !(ctx.alive &= ~hit)) return;")
         body.append("    }")
         body.append("}")
 
-    for l in fine_defs:
-        w(l)
-    w("")
+    w(f"""    // Fine environment tests of the spheres EnvFine[k0..k1) of one frame, for the segments in
+    // `need`: the segments whose block collides.
+    template <int W>
+    static __device__ __noinline__ unsigned env_fine(const vg::EnvView &ev, const vg::Frame f, int k0, int k1, unsigned need)
+    {{
+        unsigned dead = 0u;
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k)
+        {{
+            const float4 o = {pre}SlotOff[{pre}EnvFine[k]];
+            const float4 c = vg::frame_point(f, o);
+            const unsigned hit = vg::env_query_inline<W>(ev, c.x, c.y, c.z, c.w, need);
+            dead |= hit;
+            need &= ~hit;
+            if (!need)
+            {{
+                break;
+            }}
+        }}
+        return dead;
+    }}
+
+    // OR of the sign bits of the fine self-collision tests of pairs[k0..k1) (slot ids), the first
+    // slot of each pair in frame a, the second in frame b.
+    static __device__ __noinline__ unsigned self_pairs(const vg::Frame a, const vg::Frame b, const int2 *pairs, int k0, int k1)
+    {{
+        unsigned acc = 0u;
+        int last = -1;
+        float4 ca = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k)
+        {{
+            const int2 pr = pairs[k];
+            if (pr.x != last)
+            {{
+                ca = vg::frame_point(a, {pre}SlotOff[pr.x]);
+                last = pr.x;
+            }}
+            const float4 cb = vg::frame_point(b, {pre}SlotOff[pr.y]);
+            acc |= vg::self_bits(ca.x, ca.y, ca.z, cb.x, cb.y, cb.z, __fadd_rn(ca.w, cb.w));
+        }}
+        return acc;
+    }}
+""")
     w("    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.")
     w("    template <typename Ctx>")
     w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
@@ -716,7 +809,7 @@ def gen_c(model: dict) -> str:
     w("")
 
     for tgt, ty, sc in (("c32", "float", "vgo_sincos_ref"), ("c64", "double", None)):
-        em = Emitter(tgt, 1e-9 if tgt == "c32" else 0.0)
+        em = Emitter(tgt, SNAP32 if tgt == "c32" else 0.0)
         if tgt == "c32":
             scf = lambda x, s, c: f"float {s}, {c}; vgo_sincos_ref({x}, &{s}, &{c});"
         else:
