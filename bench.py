@@ -267,6 +267,7 @@ def run_gpu(args, world, rank, local):
     dev = torch.device("cuda", local)
     scene, a_np, b_np = workload()
     env = vg.Environment.from_scene(scene)
+    env.set_schedule(args.schedule)
     a = torch.from_numpy(a_np).to(dev)
     b = torch.from_numpy(b_np).to(dev)
     out = torch.empty(N_EDGES, dtype=torch.uint8, device=dev)
@@ -333,7 +334,7 @@ def run_gpu(args, world, rank, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded scene and edges)",
-        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "order": "plain (reference block order)",
+        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "order": "plain (reference block order)", "schedule": "warp per edge" if args.schedule == 1 else "lane-block per edge",
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
                    "colliding_fraction": float(1 - gpu_verdicts.mean())},
         "gpu_launches": args.steps,
@@ -361,6 +362,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    ap.add_argument("--schedule", type=int, default=1, help="GPU edge schedule: 1 warp per edge, 0 lane-block per edge")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

@@ -69,6 +69,10 @@ int vg_env_add_capsule(vg_env *env, const float *fields8);
 int vg_env_add_cuboid(vg_env *env, const float *fields15);
 /* Which reference build to reproduce: lanes 8 + VG_SQRT_X86 (default) or lanes 4 + VG_SQRT_EXACT. */
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
+/* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):
+ * 1 (default) = a warp checks consecutive blocks of one edge, 0 = each lane-block checks its own
+ * edge.  No reference counterpart: the reference validates one edge at a time on one core. */
+int vg_env_set_schedule(vg_env *env, int schedule);
 /* Number of objects of a kind (0 spheres, 1 capsules, 2 z-capsules, 3 cuboids, 4 z-cuboids)
  * and the fields of one, in checking order, followed by its min_distance. */
 int vg_env_count(const vg_env *env, int kind, size_t *count);

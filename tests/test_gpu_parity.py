@@ -176,3 +176,25 @@ def test_bad_arguments_raise(vg):
     q = np.zeros((4, 7), np.float32)
     with pytest.raises(vg.VampError):
         vg.panda.validate_motion_batch(q, q, env, resolution=0)
+
+
+@pytest.mark.parametrize("lanes,sqrt_mode", [(8, 0), (4, 1)])
+def test_both_edge_schedules_agree_with_the_oracle(vg, port, torch, lanes, sqrt_mode):
+    """A warp per edge (consecutive blocks) and a lane-block per edge give the same verdicts
+    and the same reference block counts."""
+    from oracle.vgo import SQRT_EXACT, SQRT_X86
+    from vamp_gb300 import scenes
+
+    scene = scenes.scene_config1(8)
+    rb = port.robot("panda")
+    a, b = scenes.edges(rb.s_m, rb.s_a, 8192, 88)
+    cpu, cpu_blocks = port.env(scene, sqrt_mode=SQRT_X86 if sqrt_mode == 0 else SQRT_EXACT).validate_motions(
+        rb, a, b, 32, lanes=lanes, threads=THREADS)
+    for schedule in (0, 1):
+        env = vg.Environment.from_scene(scene, lanes=lanes, sqrt_mode=sqrt_mode)
+        env.set_schedule(schedule)
+        blocks = torch.zeros(len(a), dtype=torch.int32, device="cuda")
+        gpu = vg.panda.validate_motion_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), env, 32,
+                                             blocks=blocks).cpu().numpy()
+        assert np.array_equal(gpu, cpu), schedule
+        assert np.array_equal(blocks.cpu().numpy(), cpu_blocks), schedule

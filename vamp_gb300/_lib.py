@@ -43,6 +43,7 @@ def _load() -> ctypes.CDLL:
         "vg_env_add_capsule": ([_p, _p], _i),
         "vg_env_add_cuboid": ([_p, _p], _i),
         "vg_env_set_mode": ([_p, _i, _i], _i),
+        "vg_env_set_schedule": ([_p, _i], _i),
         "vg_env_count": ([_p, _i, _p], _i),
         "vg_env_get": ([_p, _i, _sz, _p], _i),
         "vg_validate_states_device": ([_s, _p, _p, _sz, _p, _p], _i),
@@ -82,6 +83,7 @@ EXPORTED = (
     "vg_env_add_capsule",
     "vg_env_add_cuboid",
     "vg_env_set_mode",
+    "vg_env_set_schedule",
     "vg_env_count",
     "vg_env_get",
     "vg_validate_states_device",

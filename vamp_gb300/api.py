@@ -67,6 +67,10 @@ class Environment:
         check(lib.vg_env_set_mode(self._h, lanes, sqrt_mode))
         self.lanes, self.sqrt_mode = lanes, sqrt_mode
 
+    def set_schedule(self, schedule: int) -> None:
+        """GPU edge schedule: 1 (default) a warp per edge, 0 a lane-block per edge."""
+        check(lib.vg_env_set_schedule(self._h, schedule))
+
     def add_sphere(self, sphere) -> None:
         f = np.ascontiguousarray(_fields(sphere, ("x", "y", "z", "r")), np.float32)
         check(lib.vg_env_add_sphere(self._h, _ptr(f)))

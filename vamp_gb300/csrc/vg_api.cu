@@ -389,6 +389,14 @@ int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode)
     return VG_OK;
 }
 
+int vg_env_set_schedule(vg_env *env, int schedule)
+{
+    if (!env || (schedule != 0 && schedule != 1))
+        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0 or 1");
+    env->schedule = schedule;
+    return VG_OK;
+}
+
 int vg_env_count(const vg_env *env, int kind, size_t *count)
 {
     if (!env || kind < 0 || kind > 4 || !count)
@@ -450,16 +458,20 @@ int vg_validate_motions_device(
         return rc;
     const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
     const int which = env->lanes == 8 ? 0 : 1;
+    const bool grouped = env->schedule == 1;
+    const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];
     int occ = 0;
-    if (int rc = prepare_kernel(r->edges_fn[which], smem, kBlock, &occ))
+    if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
         return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
-    const int segs_per_block = kBlock / env->lanes;
-    const long long want = (static_cast<long long>(n) + segs_per_block - 1) / segs_per_block;
+    // edges handled at once by one block of threads: a warp each (same-edge schedule) or a
+    // segment each
+    const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
+    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
     const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
     EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env)};
-    VG_CUDA(r->edges[which](p, grid, kBlock, smem, s), "edges kernel launch");
+    VG_CUDA((grouped ? r->edges_grouped[which] : r->edges[which])(p, grid, kBlock, smem, s), "edges kernel launch");
     return VG_OK;
 }
 

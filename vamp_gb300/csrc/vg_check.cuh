@@ -338,7 +338,9 @@ namespace vg
             const float v = __fmaf_rn(c.x, c.x, __fmaf_rn(c.z, c.z, __fmul_rn(c.y, c.y)));
             const float m = seg_max<W>(max_extent(e, v, c.w));
             M[s] = on ? m : -__int_as_float(0x7f800000);
-            Mw[s] = warp_max(M[s]);
+            // max_extent is >= 0 (or +inf): as unsigned integers its bit patterns order like the
+            // floats, so one warp reduction gives the warp-wide bound (inactive lanes count as 0)
+            Mw[s] = __uint_as_float(__reduce_max_sync(kFull, on ? __float_as_uint(m) : 0u));
             Mall = fmaxf(Mall, Mw[s]);
             bits[s] = 0u;
         }

@@ -24,6 +24,9 @@ namespace vg
         // edges: index 0 = 8-lane blocks, 1 = 4-lane blocks
         cudaError_t (*edges[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_fn[2];
+        // same-edge schedule (a warp checks consecutive blocks of one edge)
+        cudaError_t (*edges_grouped[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_grouped_fn[2];
         cudaError_t (*spheres)(const float *, long long, float *, cudaStream_t);
     };
 
@@ -41,6 +44,7 @@ struct vg_env
     std::vector<float> obj[5];
     int lanes = 8;
     int sqrt_mode = 0;
+    int schedule = 1;  // 0: a segment per edge, 1: a warp per edge (consecutive blocks)
     bool dirty = true;
     int device = -1;
     // device image

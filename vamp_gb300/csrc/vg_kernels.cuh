@@ -16,7 +16,7 @@
 
 // Resident blocks of 128 threads per SM the kernels are compiled for (caps their registers).
 #ifndef VG_MIN_BLOCKS
-#define VG_MIN_BLOCKS 1
+#define VG_MIN_BLOCKS 3
 #endif
 
 namespace vg
@@ -233,6 +233,101 @@ namespace vg
             if (need)
             {
                 refill(need);
+            }
+        }
+    }
+
+    // Same-edge schedule: a warp owns one edge at a time and its 32 / W segments check
+    // consecutive blocks i0, i0 + 1, ... of it.  Lanes that stand for neighbouring blocks sit at
+    // almost the same configurations, so the warp's union of control flow is close to a single
+    // block's.  Each segment reaches its block by the same repeated subtraction as the reference
+    // (block i = block 0 minus v / (W n), i times).  The edge is invalid if any checked block is,
+    // and the reference would have stopped at the first invalid block, so the block count
+    // reported is that block's index + 1.
+    template <typename Robot, int W>
+    __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_grouped_kernel(EdgesParams p)
+    {
+        extern __shared__ float4 smem[];
+        const EnvView ev = stage_env(p.env, smem);
+        constexpr int D = Robot::kDim;
+        constexpr int S = 32 / W;                 // segments (blocks) per warp
+        const int lane = threadIdx.x & 31;
+        const int seg = lane / W;
+        const int sl = lane % W;
+        const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
+        constexpr unsigned kSegBits = W == 32 ? kFull : ((1u << W) - 1u);
+
+        for (;;)
+        {
+            unsigned got = 0;
+            if (lane == 0)
+            {
+                got = atomicAdd(p.head, 1u);
+            }
+            got = __shfl_sync(kFull, got, 0);
+            if (got >= static_cast<unsigned>(p.n))
+            {
+                break;
+            }
+            const int e = static_cast<int>(got);
+            float q[D], bs[D], v[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                const float av = p.a[static_cast<long long>(e) * D + d];
+                v[d] = __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
+                q[d] = __fmaf_rn(v[d], pct, av);
+            }
+            const float len = edge_length<D>(v);
+            const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
+            const float nf = ceilf(t);
+            const int n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
+            const float denom = static_cast<float>(W * n);
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                bs[d] = __fdiv_rn(v[d], denom);
+            }
+            // segment `seg` starts at block `seg`
+            for (int k = 0; k < seg; ++k)
+            {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                {
+                    q[d] = __fsub_rn(q[d], bs[d]);
+                }
+            }
+            int verdict = 1, checked = n;
+            for (int i0 = 0; i0 < n; i0 += S)
+            {
+                const bool active = i0 + seg < n;
+                const unsigned mask = __ballot_sync(kFull, active);
+                const unsigned alive = run_fkcc<Robot, W>(ev, q, mask);
+                const unsigned dead = mask & ~alive;
+                if (dead)
+                {
+                    verdict = 0;
+                    checked = i0 + (__ffs(dead) - 1) / W + 1;
+                    break;
+                }
+#pragma unroll 1
+                for (int k = 0; k < S; ++k)
+                {
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        q[d] = __fsub_rn(q[d], bs[d]);
+                    }
+                }
+            }
+            (void)kSegBits;
+            if (lane == 0)
+            {
+                p.out[e] = static_cast<uint8_t>(verdict);
+                if (p.blocks)
+                {
+                    p.blocks[e] = checked;
+                }
             }
         }
     }

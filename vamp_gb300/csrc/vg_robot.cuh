@@ -20,6 +20,13 @@ namespace vg
         return cudaGetLastError();
     }
 
+    template <typename R, int W>
+    cudaError_t launch_edges_grouped(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        edges_grouped_kernel<R, W><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
     template <typename R>
     cudaError_t launch_spheres(const float *q, long long n, float *out, cudaStream_t s)
     {
@@ -51,6 +58,10 @@ namespace vg
         o.edges[1] = &launch_edges<R, 4>;
         o.edges_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8>);
         o.edges_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4>);
+        o.edges_grouped[0] = &launch_edges_grouped<R, 8>;
+        o.edges_grouped[1] = &launch_edges_grouped<R, 4>;
+        o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8>);
+        o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4>);
         o.spheres = &launch_spheres<R>;
         return o;
     }
