@@ -101,6 +101,28 @@ int vg_validate_motions_device(
     int32_t *blocks,
     void *stream);
 
+/* Allocation-free form of vg_validate_motions_device, for callers that must not allocate GPU
+ * memory while they run (a real-time planner that reserves all memory up front so no call can
+ * block on the allocator or run out of memory mid-plan; a framework that owns device memory
+ * through its own pool).  No counterpart in the reference, which runs on the CPU.  Same verdicts
+ * and block counts; allocates nothing.  Its only scratch, the edge kernel's work counter, is a
+ * fixed 256-byte device array inside the library that every GPU loading the library keeps until
+ * exit.  Requirements: env already uploaded to the current device by an earlier ordinary check
+ * call and unchanged since (VG_ERR_STATE otherwise); n <= 2^31 - 1 (VG_ERR_LIMIT).  The first
+ * call on each device looks up the array's device address: make it before any stream capture.
+ * All calls share the array (the counter is cleared on `stream` before each launch): calls whose
+ * kernels overlap on the GPU race, so issue them on one stream or wait between them. */
+int vg_validate_motions_device_noalloc(
+    const char *robot,
+    const vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream);
+
 /* Sphere centres and radii of every sphere slot (fine spheres, then each checked link's coarse
  * sphere), out is [n][slots][4].  Replaces Robot::sphere_fk (robots/panda.hh:117-462). */
 int vg_sphere_fk_device(const char *robot, const float *q, size_t n, float *out, void *stream);

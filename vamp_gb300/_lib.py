@@ -48,6 +48,7 @@ def _load() -> ctypes.CDLL:
         "vg_env_get": ([_p, _i, _sz, _p], _i),
         "vg_validate_states_device": ([_s, _p, _p, _sz, _p, _p], _i),
         "vg_validate_motions_device": ([_s, _p, _p, _p, _sz, _i, _p, _p, _p], _i),
+        "vg_validate_motions_device_noalloc": ([_s, _p, _p, _p, _sz, _i, _p, _p, _p], _i),
         "vg_sphere_fk_device": ([_s, _p, _sz, _p, _p], _i),
         "vg_validate_states": ([_s, _p, _p, _sz, _p], _i),
         "vg_validate_motions": ([_s, _p, _p, _p, _sz, _i, _p], _i),
@@ -88,6 +89,7 @@ EXPORTED = (
     "vg_env_get",
     "vg_validate_states_device",
     "vg_validate_motions_device",
+    "vg_validate_motions_device_noalloc",
     "vg_sphere_fk_device",
     "vg_validate_states",
     "vg_validate_motions",

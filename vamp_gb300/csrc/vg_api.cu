@@ -265,6 +265,44 @@ namespace vg
     }
 
     constexpr int kBlock = 128;
+
+    // ------------------------------------------------------------ allocation-free variant
+    //
+    // Scratch for vg_validate_motions_device_noalloc: the edge kernel's work counter lives in
+    // this fixed array instead of memory the library allocates.  Every GPU that loads the
+    // library holds these bytes until the process exits.  All calls share it: the counter is
+    // cleared on the caller's stream before each launch, and calls whose kernels overlap on the
+    // GPU race on it.
+    constexpr size_t kNoAllocScratchBytes = 256;
+    static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+    static_assert(sizeof(unsigned) <= kNoAllocScratchBytes, "the work counter must fit the scratch array");
+
+    // Device address of the scratch array on each device, looked up once per device with that
+    // device current (host code cannot use the array's name as a device pointer).
+    constexpr int kMaxDevices = 64;
+    static void *g_noalloc_ptr[kMaxDevices] = {};
+    static std::mutex g_noalloc_mu;
+
+    static int noalloc_scratch(int dev, void **out)
+    {
+        if (dev < 0 || dev >= kMaxDevices)
+        {
+            return set_error(VG_ERR_LIMIT, "vg_validate_motions_device_noalloc: device index above 63");
+        }
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev])
+        {
+            void *ptr = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+            {
+                return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(scratch)");
+            }
+            g_noalloc_ptr[dev] = ptr;
+        }
+        *out = g_noalloc_ptr[dev];
+        return VG_OK;
+    }
 }  // namespace vg
 
 using namespace vg;
@@ -471,6 +509,60 @@ int vg_validate_motions_device(
     const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
     const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
     EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env)};
+    VG_CUDA((grouped ? r->edges_grouped[which] : r->edges[which])(p, grid, kBlock, smem, s), "edges kernel launch");
+    return VG_OK;
+}
+
+// For callers that must not allocate GPU memory while they run, e.g. a real-time planner that
+// reserves all memory up front so that no call can block on the allocator or fail for lack of
+// memory mid-plan, or a host framework that owns the device memory through its own pool.  Same
+// verdicts and block counts as vg_validate_motions_device; the work counter lives in the
+// library's fixed scratch array.  Allocates nothing: no cudaMalloc, cudaFree or allocating
+// library call.  The environment must already be uploaded to the current device by an earlier
+// ordinary check call (vg_validate_motions_device, vg_validate_states_device, or their host
+// forms) and not changed since.  The first call on each device looks up the scratch array's
+// device address; make that first call before any stream capture.  Calls whose kernels overlap
+// on the GPU race on the shared counter: issue them on one stream, or wait between them.
+int vg_validate_motions_device_noalloc(
+    const char *robot,
+    const vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!a || !b || !out)) || resolution < 1)
+        return set_error(VG_ERR_ARG, "vg_validate_motions_device_noalloc: bad argument");
+    if (n > 0x7fffffffu)
+        return set_error(VG_ERR_LIMIT, "vg_validate_motions_device_noalloc: more than 2^31 - 1 edges (the 32-bit work counter's limit)");
+    int dev = 0;
+    VG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!env->d_image || env->dirty || env->device != dev)
+        return set_error(VG_ERR_STATE, "vg_validate_motions_device_noalloc: the environment is not uploaded to this device "
+                                       "(run an ordinary check call with it first, after its last change)");
+    void *scratch = nullptr;
+    if (int rc = noalloc_scratch(dev, &scratch))
+        return rc;
+    if (n == 0)
+        return VG_OK;
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int which = env->lanes == 8 ? 0 : 1;
+    const bool grouped = env->schedule == 1;
+    const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];
+    int occ = 0;
+    if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
+        return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned *counter = static_cast<unsigned *>(scratch);
+    VG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "clear scratch counter");
+    const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
+    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
+    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, counter, env_device(env)};
     VG_CUDA((grouped ? r->edges_grouped[which] : r->edges[which])(p, grid, kBlock, smem, s), "edges kernel launch");
     return VG_OK;
 }
