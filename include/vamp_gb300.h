@@ -67,6 +67,17 @@ int vg_env_add_capsule(vg_env *env, const float *fields8);
 /* Cuboid: centre xyz, axis_1 xyz, axis_2 xyz, axis_3 xyz, half extents (collision/shapes.hh:29-120);
  * stored as z-aligned when axis_3_z == 1 (bindings/environment.cc:118-131). */
 int vg_env_add_cuboid(vg_env *env, const float *fields15);
+/* A pointcloud, checked as a CAPT built exactly as the reference builds it
+ * (collision/capt.hh:294-365; Environment.add_pointcloud, bindings/environment.cc:150-161):
+ * xyz is [n][3], n >= 2; queries pad sphere radii by r_point; the tree affords points for radii
+ * up to r_max.  At most 4 pointclouds per environment. */
+int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point);
+/* The tree of the index-th pointcloud (collision/capt.hh:584-617): sizes = {nlog2, tests,
+ * leaves, 8-point blocks}; then, if non-NULL, tests[tests], aabbs[leaves][6], aff_starts[leaves
+ * + 1], aff[blocks][3][8] (x, y, z planes of each block), top[6].  Call with NULL arrays for the
+ * sizes. */
+int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, float *tests, float *aabbs,
+                             uint32_t *aff_starts, float *aff, float *top);
 /* Which reference build to reproduce: lanes 8 + VG_SQRT_X86 (default) or lanes 4 + VG_SQRT_EXACT. */
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
 /* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):

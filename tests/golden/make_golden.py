@@ -125,6 +125,20 @@ def main():
     lay = ref.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS)
     np.savez_compressed(OUT / "capt_layout.npz", points=pts, r=np.array([0.012, 0.08, scenes.POINT_RADIUS], np.float32), **lay)
 
+    # --- pointcloud scenes: verdicts through the reference's CAPT (capt.hh:425-506)
+    rb = port.robot("panda")
+    cloud = scenes.surface_pointcloud(61, n_points=10000)
+    scene = {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+             "cuboids": np.zeros((0, 15), np.float32),
+             "pointclouds": [{"points": cloud, "r_min": 0.012, "r_max": 0.08, "r_point": scenes.POINT_RADIUS}]}
+    renv = ref.env(scene)
+    q = scenes.configurations(rb.s_m, rb.s_a, 1024, 62)
+    sv = renv.validate_states("panda", q)
+    ea, eb = scenes.edges(rb.s_m, rb.s_a, 512, 63)
+    ev = renv.validate_motions("panda", ea, eb, 32)
+    np.savez_compressed(OUT / "cloud_panda.npz", points=cloud, r=np.array([0.012, 0.08, scenes.POINT_RADIUS], np.float32),
+                        q=q, state_verdict=sv, a=ea, b=eb, edge_verdict=ev)
+
     print("golden fixtures written to", OUT)
 
 

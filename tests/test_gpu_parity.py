@@ -198,3 +198,46 @@ def test_both_edge_schedules_agree_with_the_oracle(vg, port, torch, lanes, sqrt_
                                              blocks=blocks).cpu().numpy()
         assert np.array_equal(gpu, cpu), schedule
         assert np.array_equal(blocks.cpu().numpy(), cpu_blocks), schedule
+
+
+def _cloud(points, r_min=0.012, r_max=0.08):
+    from vamp_gb300 import scenes
+
+    return {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+            "cuboids": np.zeros((0, 15), np.float32),
+            "pointclouds": [{"points": points, "r_min": r_min, "r_max": r_max, "r_point": scenes.POINT_RADIUS}]}
+
+
+def test_pointcloud_verdicts_match_reference_and_oracle(vg, port):
+    g = golden("cloud_panda")
+    scene = _cloud(g["points"], float(g["r"][0]), float(g["r"][1]))
+    env = vg.Environment.from_scene(scene)
+    penv = port.env(scene)
+    rb = port.robot("panda")
+    gs = vg.panda.validate_batch(g["q"], env)
+    assert np.array_equal(gs, penv.validate_states(rb, g["q"]))
+    assert np.array_equal(gs, g["state_verdict"])
+    ge = vg.panda.validate_motion_batch(g["a"], g["b"], env, 32)
+    cpu, _ = penv.validate_motions(rb, g["a"], g["b"], 32)
+    assert np.array_equal(ge, cpu)
+    assert np.array_equal(ge, g["edge_verdict"])
+
+
+def test_pointcloud_with_primitives_is_the_oracles(vg, port, torch):
+    """50,000 surface points plus the workspace primitives; states and edges."""
+    from vamp_gb300 import scenes
+
+    scene = scenes.scene_config1(3)
+    scene["pointclouds"] = _cloud(scenes.surface_pointcloud(9, 50000))["pointclouds"]
+    rb = port.robot("panda")
+    env = vg.Environment.from_scene(scene)
+    penv = port.env(scene)
+    q = scenes.configurations(rb.s_m, rb.s_a, 8192, 91)
+    assert np.array_equal(vg.panda.validate_batch(q, env), penv.validate_states(rb, q, threads=THREADS))
+    a, b = scenes.edges(rb.s_m, rb.s_a, 4096, 92)
+    blocks = torch.zeros(len(a), dtype=torch.int32, device="cuda")
+    gpu = vg.panda.validate_motion_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), env, 32,
+                                         blocks=blocks).cpu().numpy()
+    cpu, cpu_blocks = penv.validate_motions(rb, a, b, 32, threads=THREADS)
+    assert np.array_equal(gpu, cpu)
+    assert np.array_equal(blocks.cpu().numpy(), cpu_blocks)

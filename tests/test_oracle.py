@@ -107,3 +107,39 @@ def test_threads_do_not_change_verdicts(port):
     one, b1 = env.validate_motions(rb, g["a"], g["b"], 32, threads=1)
     many, b4 = env.validate_motions(rb, g["a"], g["b"], 32, threads=4)
     assert np.array_equal(one, many) and np.array_equal(b1, b4)
+
+
+def _cloud_scene(g):
+    return {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+            "cuboids": np.zeros((0, 15), np.float32),
+            "pointclouds": [{"points": g["points"], "r_min": float(g["r"][0]), "r_max": float(g["r"][1]),
+                             "r_point": float(g["r"][2])}]}
+
+
+def test_pointcloud_verdicts_match_reference(port):
+    g = golden("cloud_panda")
+    env = port.env(_cloud_scene(g))
+    rb = port.robot("panda")
+    assert np.array_equal(env.validate_states(rb, g["q"]), g["state_verdict"])
+    ev, _ = env.validate_motions(rb, g["a"], g["b"], 32)
+    assert np.array_equal(ev, g["edge_verdict"])
+
+
+def test_library_capt_layout_is_the_reference_bit_for_bit(port):
+    """The shipped library's host-side CAPT builder against the reference's layout and the
+    oracle's (no GPU needed)."""
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+
+    g = golden("capt_layout")
+    env = vg.Environment()
+    env.add_pointcloud(g["points"], *map(float, g["r"]))
+    lay = env.pointcloud_layout(0)
+    for k in ("tests", "aabbs", "aff_starts", "aff", "top"):
+        assert np.array_equal(lay[k], g[k], equal_nan=True), k
+    pts = scenes.surface_pointcloud(7, 20000)
+    env = vg.Environment()
+    env.add_pointcloud(pts, 0.012, 0.08, scenes.POINT_RADIUS)
+    mine, ref = env.pointcloud_layout(0), port.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS)
+    for k in ("tests", "aabbs", "aff_starts", "aff", "top"):
+        assert np.array_equal(mine[k], ref[k], equal_nan=True), k

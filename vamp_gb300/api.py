@@ -96,9 +96,26 @@ class Environment:
             env.add_capsule(c)
         for c in np.asarray(scene.get("cuboids", np.zeros((0, 15))), np.float32):
             env.add_cuboid(c)
-        if scene.get("pointclouds"):
-            raise VampError("pointclouds are not supported by this build")
+        for pc in scene.get("pointclouds", []):
+            env.add_pointcloud(pc["points"], pc["r_min"], pc["r_max"], pc["r_point"])
         return env
+
+    def add_pointcloud(self, points, r_min: float, r_max: float, r_point: float) -> None:
+        """A pointcloud checked as a CAPT (collision/capt.hh), built on the host."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        check(lib.vg_env_add_pointcloud(self._h, _ptr(pts), len(pts), float(r_min), float(r_max), float(r_point)))
+
+    def pointcloud_layout(self, index: int = 0) -> dict:
+        sizes = np.zeros(4, np.uint64)
+        nul = ctypes.c_void_p()
+        check(lib.vg_env_pointcloud_layout(self._h, index, _ptr(sizes), nul, nul, nul, nul, nul))
+        nlog2, nt, nl, nb = (int(v) for v in sizes)
+        out = dict(nlog2=nlog2, tests=np.zeros(nt, np.float32), aabbs=np.zeros((nl, 6), np.float32),
+                   aff_starts=np.zeros(nl + 1, np.uint32), aff=np.zeros((nb, 3, 8), np.float32), top=np.zeros(6, np.float32))
+        check(lib.vg_env_pointcloud_layout(self._h, index, _ptr(sizes), _ptr(out["tests"]), _ptr(out["aabbs"]),
+                                           _ptr(out["aff_starts"]), _ptr(out["aff"]), _ptr(out["top"])))
+        out["aff"] = out["aff"].transpose(1, 0, 2).copy()  # [3][blocks][8], as the oracle dumps it
+        return out
 
     def objects(self, kind: int) -> np.ndarray:
         """Fields of every object of a kind in checking order, min_distance last."""

@@ -165,6 +165,65 @@ namespace vg
         }
     }
 
+    static_assert(sizeof(CaptView) % sizeof(float4) == 0, "CaptView must pack into float4s");
+
+    // Uploads each pointcloud's tree once (4 device buffers per cloud).
+    static int upload_clouds(vg_env *e)
+    {
+        while (e->d_clouds.size() < 4 * e->clouds.size())
+        {
+            const CaptHost &c = e->clouds[e->d_clouds.size() / 4];
+            const void *src[4] = {c.tests.data(), c.aabbs.data(), c.aff_starts.data(), c.aff.data()};
+            const size_t bytes[4] = {c.tests.size() * sizeof(float), c.aabbs.size() * sizeof(float),
+                                     c.aff_starts.size() * sizeof(uint32_t), std::max<size_t>(16, c.aff.size() * sizeof(float))};
+            void *dst[4] = {nullptr, nullptr, nullptr, nullptr};
+            for (int k = 0; k < 4; ++k)
+            {
+                cudaError_t err = cudaMalloc(&dst[k], bytes[k]);
+                if (err == cudaSuccess && src[k] && (k != 3 || !c.aff.empty()))
+                {
+                    err = cudaMemcpy(dst[k], src[k], k == 3 ? c.aff.size() * sizeof(float) : bytes[k], cudaMemcpyHostToDevice);
+                }
+                if (err != cudaSuccess)
+                {
+                    for (int j = 0; j <= k; ++j)
+                    {
+                        if (dst[j])
+                            cudaFree(dst[j]);
+                    }
+                    return cuda_fail(err, "upload pointcloud");
+                }
+            }
+            for (int k = 0; k < 4; ++k)
+            {
+                e->d_clouds.push_back(dst[k]);
+            }
+        }
+        return VG_OK;
+    }
+
+    static void pack_clouds(const vg_env *e, std::vector<float4> &img, int *cloud_off)
+    {
+        *cloud_off = static_cast<int>(img.size());
+        for (size_t i = 0; i < e->clouds.size(); ++i)
+        {
+            const CaptHost &c = e->clouds[i];
+            CaptView v{};
+            v.tests = static_cast<const float *>(e->d_clouds[4 * i + 0]);
+            v.aabbs = static_cast<const float *>(e->d_clouds[4 * i + 1]);
+            v.starts = static_cast<const uint32_t *>(e->d_clouds[4 * i + 2]);
+            v.aff = static_cast<const float4 *>(e->d_clouds[4 * i + 3]);
+            for (int k = 0; k < 6; ++k)
+                v.top[k] = c.top[k];
+            v.r_point = c.r_point;
+            v.nlog2 = c.nlog2;
+            v.n_tests = static_cast<int>(c.tests.size());
+            const size_t at = img.size();
+            img.resize(at + sizeof(CaptView) / sizeof(float4));
+            std::memcpy(&img[at], &v, sizeof(CaptView));
+        }
+    }
+
     // Uploads the environment image if it changed; records the current device.
     static int commit(vg_env *e)
     {
@@ -178,8 +237,11 @@ namespace vg
         {
             return set_error(VG_ERR_STATE, "environment was committed on another device");
         }
+        if (int rc = upload_clouds(e))
+            return rc;
         std::vector<float4> img;
         pack_image(e, img, e->off, e->n);
+        pack_clouds(e, img, &e->cloud_off);
         if (img.size() > e->image_cap)
         {
             if (e->d_image)
@@ -212,6 +274,8 @@ namespace vg
             d.off[k] = e->off[k];
         }
         d.sqrt_mode = e->sqrt_mode;
+        d.n_clouds = static_cast<int>(e->clouds.size());
+        d.cloud_off = e->cloud_off;
         return d;
     }
 
@@ -376,6 +440,8 @@ void vg_env_destroy(vg_env *env)
         cudaFree(env->d_counter);
     if (env->d_stage)
         cudaFree(env->d_stage);
+    for (void *p : env->d_clouds)
+        cudaFree(p);
     delete env;
 }
 
@@ -411,6 +477,51 @@ int vg_env_add_cuboid(vg_env *env, const float *f)
     row[15] = cuboid_min_distance(f);
     insert_sorted(env->obj[f[11] == 1.0f ? 4 : 3], 15, row);
     env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point)
+{
+    if (!env || !xyz || n < 2 || !(r_min >= 0.0f) || !(r_max >= r_min) || !(r_point >= 0.0f))
+        return set_error(VG_ERR_ARG, "vg_env_add_pointcloud: need at least 2 points and 0 <= r_min <= r_max, r_point >= 0");
+    if (env->clouds.size() >= static_cast<size_t>(kMaxClouds))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud: at most 4 pointclouds per environment");
+    if (n > (size_t{1} << 30))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud: at most 2^30 points");
+    try
+    {
+        CaptHost c;
+        capt_build(xyz, n, r_min, r_max, r_point, c);
+        env->clouds.push_back(std::move(c));
+    }
+    catch (...)
+    {
+        return set_error(VG_ERR_NOMEM, "vg_env_add_pointcloud: out of host memory");
+    }
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, float *tests, float *aabbs,
+                             uint32_t *aff_starts, float *aff, float *top)
+{
+    if (!env || !sizes || index < 0 || static_cast<size_t>(index) >= env->clouds.size())
+        return set_error(VG_ERR_ARG, "vg_env_pointcloud_layout: bad argument");
+    const CaptHost &c = env->clouds[index];
+    sizes[0] = static_cast<uint64_t>(c.nlog2);
+    sizes[1] = c.tests.size();
+    sizes[2] = c.aabbs.size() / 6;
+    sizes[3] = c.blocks();
+    if (tests)
+        std::memcpy(tests, c.tests.data(), c.tests.size() * sizeof(float));
+    if (aabbs)
+        std::memcpy(aabbs, c.aabbs.data(), c.aabbs.size() * sizeof(float));
+    if (aff_starts)
+        std::memcpy(aff_starts, c.aff_starts.data(), c.aff_starts.size() * sizeof(uint32_t));
+    if (aff)
+        std::memcpy(aff, c.aff.data(), c.aff.size() * sizeof(float));
+    if (top)
+        std::memcpy(top, c.top, sizeof(c.top));
     return VG_OK;
 }
 

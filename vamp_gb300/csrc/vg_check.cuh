@@ -167,12 +167,30 @@ namespace vg
         return kind == 0 ? 4 : (kind <= 2 ? 8 : 15);
     }
 
+    // One pointcloud's CAPT on the device (collision/capt.hh:584-617): split values, leaf boxes,
+    // per-leaf ranges of 8-point affordance blocks (x[8] y[8] z[8] = 6 float4 per block).
+    struct CaptView
+    {
+        const float *tests;
+        const float *aabbs;
+        const uint32_t *starts;
+        const float4 *aff;
+        float top[6];
+        float r_point;
+        int nlog2;
+        int n_tests;
+        int pad[3];
+    };
+    constexpr int kMaxClouds = 4;
+
     struct EnvView
     {
         const float4 *rec[5];
         int n[5];
         const uint32_t *rsqrt_tab;
         int sqrt_mode;
+        const CaptView *clouds;
+        int n_clouds;
     };
 
     __device__ __forceinline__ float sql2(float ax, float ay, float az, float bx, float by, float bz)
@@ -315,6 +333,74 @@ namespace vg
         }
     }
 
+    // CAPT::collides_simd (collision/capt.hh:425-506) for one lane's sphere: true if the lane
+    // hits.  The reference's block result is the OR over its lanes; its early exits (no lane in
+    // the top box, no lane in its leaf box) return false for exactly the lanes that would not
+    // hit, so the per-lane form is the same test.
+    __device__ __forceinline__ bool capt_lane(const CaptView &c, float x, float y, float z, float r)
+    {
+        const float rad = __fadd_rn(r, c.r_point);
+        const float p[3] = {x, y, z};
+        bool in = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            in &= (__fadd_rn(p[k], rad) >= c.top[k]) & (__fsub_rn(p[k], rad) <= c.top[3 + k]);
+        }
+        if (!in)
+        {
+            return false;
+        }
+        int idx = 0;
+        int k = 0;
+#pragma unroll 1
+        for (int i = 0; i < c.nlog2; ++i)
+        {
+            const float pk = k == 0 ? x : (k == 1 ? y : z);
+            idx = 2 * idx + 1 + (pk >= __ldg(c.tests + idx) ? 1 : 0);
+            k = k == 2 ? 0 : k + 1;
+        }
+        const int leaf = idx - c.n_tests;
+        const float *box = c.aabbs + 6 * static_cast<long long>(leaf);
+        float d[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+            const float lo = __ldg(box + j), hi = __ldg(box + 3 + j);
+            const float m = p[j] > lo ? p[j] : lo;
+            const float cl = m < hi ? m : hi;
+            d[j] = __fsub_rn(p[j], cl);
+        }
+        const float rc = __fmul_rn(rad, rad);
+        if (!(__fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmul_rn(d[0], d[0]))) <= rc))
+        {
+            return false;
+        }
+        const uint32_t b0 = __ldg(c.starts + leaf), b1 = __ldg(c.starts + leaf + 1);
+#pragma unroll 1
+        for (uint32_t b = b0; b < b1; ++b)
+        {
+            const float4 *blk = c.aff + 6 * static_cast<size_t>(b);
+            const float4 xs0 = __ldg(blk + 0), xs1 = __ldg(blk + 1), ys0 = __ldg(blk + 2), ys1 = __ldg(blk + 3);
+            const float4 zs0 = __ldg(blk + 4), zs1 = __ldg(blk + 5);
+            const float ax[8] = {xs0.x, xs0.y, xs0.z, xs0.w, xs1.x, xs1.y, xs1.z, xs1.w};
+            const float ay[8] = {ys0.x, ys0.y, ys0.z, ys0.w, ys1.x, ys1.y, ys1.z, ys1.w};
+            const float az[8] = {zs0.x, zs0.y, zs0.z, zs0.w, zs1.x, zs1.y, zs1.z, zs1.w};
+            bool hit = false;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+            {
+                const float dx = __fsub_rn(ax[j], x), dy = __fsub_rn(ay[j], y), dz = __fsub_rn(az[j], z);
+                hit |= __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))) <= rc;
+            }
+            if (hit)
+            {
+                return true;
+            }
+        }
+        return false;
+    }
+
     // sphere_environment_in_collision (validity.hh:47-150) for NS spheres at once, each over the
     // segments in `mask`.  hit[s] receives the lanes of the segments whose block collides for
     // sphere s.  Warp-uniform; all 32 lanes must call.
@@ -353,6 +439,21 @@ namespace vg
         for (int s = 0; s < NS; ++s)
         {
             hit[s] = seg_any<W>(__ballot_sync(kFull, bits[s] >> 31)) & mask;
+        }
+        // pointclouds, for the blocks the primitives did not already put in collision
+#pragma unroll 1
+        for (int c = 0; c < e.n_clouds; ++c)
+        {
+#pragma unroll
+            for (int s = 0; s < NS; ++s)
+            {
+                const bool ask = on && !((hit[s] >> lane) & 1u);
+                if (__any_sync(kFull, ask))
+                {
+                    const bool h = ask && capt_lane(e.clouds[c], x[s], y[s], z[s], r[s]);
+                    hit[s] |= seg_any<W>(__ballot_sync(kFull, h)) & mask;
+                }
+            }
         }
     }
 

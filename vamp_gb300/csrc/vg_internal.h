@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "vg_capt.h"
 #include "vg_kernels.cuh"
 
 namespace vg
@@ -51,7 +52,11 @@ struct vg_env
     float4 *d_image = nullptr;
     size_t image_f4 = 0, image_cap = 0;
     int off[5] = {0, 0, 0, 0, 0};
+    int cloud_off = 0;
     int n[5] = {0, 0, 0, 0, 0};
+    // pointclouds: host trees and their device copies (tests, aabbs, starts, aff per cloud)
+    std::vector<vg::CaptHost> clouds;
+    std::vector<void *> d_clouds;  // 4 buffers per uploaded cloud
     // library-owned scratch: work counter, staging for host-pointer calls
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;

@@ -30,6 +30,8 @@ namespace vg
         int n[5];           // objects per kind
         int off[5];         // record offset of each kind, in float4 from the image start
         int sqrt_mode;
+        int n_clouds;       // CaptView descriptors at the end of the image
+        int cloud_off;      // their offset, in float4
     };
 
     constexpr int kRsqrtF4 = 2048 / 4;
@@ -44,6 +46,8 @@ namespace vg
         EnvView v;
         v.rsqrt_tab = reinterpret_cast<const uint32_t *>(smem);
         v.sqrt_mode = d.sqrt_mode;
+        v.clouds = reinterpret_cast<const CaptView *>(smem + d.cloud_off);
+        v.n_clouds = d.n_clouds;
         for (int k = 0; k < 5; ++k)
         {
             v.rec[k] = smem + d.off[k];
