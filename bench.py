@@ -224,6 +224,65 @@ def cpu_baseline(scene, a, b, budget_s: float = 10.0):
             "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
 
 
+def run_capt(args, world, rank, local):
+    """Pointcloud workload: Panda with 50,000 points sampled on the surfaces of 30 random cuboids
+    and cylinders plus 2% uniform noise, checked through the CAPT built with the Panda's radius
+    range; 1,048,576 uniform configurations and 16,384 edges at resolution 32."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300._lib import check, lib
+    from vamp_gb300.robots import model
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    m = model("panda")
+    s_m, s_a = np.array(m["s_m"], np.float32), np.array(m["s_a"], np.float32)
+    pts = scenes.surface_pointcloud(SCENE_SEED, 50_000)
+    t0 = time.perf_counter()
+    env = vg.Environment.from_scene({"pointclouds": [{"points": pts, "r_min": m["min_radius"], "r_max": m["max_radius"],
+                                                       "r_point": scenes.POINT_RADIUS}]})
+    build_s = time.perf_counter() - t0
+    q = torch.from_numpy(scenes.configurations(s_m, s_a, 1 << 20, 77)).to(dev)
+    a_np, b_np = scenes.edges(s_m, s_a, 16384, 78)
+    a, b = torch.from_numpy(a_np).to(dev), torch.from_numpy(b_np).to(dev)
+    qo = torch.empty(len(q), dtype=torch.uint8, device=dev)
+    eo = torch.empty(len(a), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def states():
+        check(lib.vg_validate_states_device(b"panda", env.handle, q.data_ptr(), len(q), qo.data_ptr(), stream.cuda_stream))
+
+    def edges():
+        check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), len(a), RESOLUTION,
+                                             eo.data_ptr(), None, stream.cuda_stream))
+
+    res = {}
+    for name, fn in (("states", states), ("edges", edges)):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            fn()
+            s1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(s0.elapsed_time(s1))
+        res[name] = float(np.mean(ts))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "pointcloud (CAPT) checks on 1 GB300", "workload": "panda + 50k surface points",
+            "states_per_s": (1 << 20) / (res["states"] / 1e3), "states_ms": res["states"],
+            "edges_per_s": 16384 / (res["edges"] / 1e3), "edges_ms": res["edges"],
+            "capt_build_s": build_s, "capt_blocks": int(env.pointcloud_layout(0)["aff_starts"][-1]),
+            "valid_states": float(qo.float().mean()), "valid_edges": float(eo.float().mean()),
+            "steps": args.steps, "warmup": args.warmup}))
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -255,6 +314,110 @@ def run_reference(args, world, rank):
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def auc(scores, positive) -> float:
+    """Area under the ROC curve: the Mann-Whitney statistic with average ranks for ties."""
+    from scipy.stats import rankdata
+
+    positive = np.asarray(positive, bool)
+    ranks = rankdata(np.asarray(scores, np.float64))
+    n_pos = int(positive.sum())
+    n_neg = len(positive) - n_pos
+    return float((ranks[positive].sum() - n_pos * (n_pos + 1) / 2.0) / max(n_pos * n_neg, 1))
+
+
+def train_predictor(env, dev, n_labels: int = 2 << 20, epochs: int = 3, seed: int = 5):
+    """The learned ordering's MLP, trained on the GPU on `n_labels` uniform Panda configurations
+    labelled by the exact checker in the benchmark scene.  Returns (mlp handle, info)."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300._lib import check, lib
+
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rb = vg.panda
+    q = torch.from_numpy(scenes.configurations(rb.s_m, rb.s_a, n_labels + 65536, seed)).to(dev)
+    valid = torch.empty(len(q), dtype=torch.uint8, device=dev)
+    check(lib.vg_validate_states_device(b"panda", env.handle, q.data_ptr(), len(q), valid.data_ptr(), stream))
+    m = lib.vg_mlp_create(7, seed)
+    losses = np.zeros(epochs, np.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    check(lib.vg_mlp_train_device(m, q.data_ptr(), valid.data_ptr(), n_labels, epochs, 1024, 1e-3, losses.ctypes.data, stream))
+    train_s = time.perf_counter() - t0
+    p = torch.empty(65536, dtype=torch.float32, device=dev)
+    held_q = q[n_labels:]
+    check(lib.vg_mlp_infer_device(m, held_q.data_ptr(), 65536, p.data_ptr(), stream))
+    torch.cuda.synchronize()
+    check(lib.vg_mlp_error(m))
+    held_auc = auc(p.cpu().numpy(), valid[n_labels:].cpu().numpy() == 0)
+    return m, {"labels": n_labels, "epochs": epochs, "batch": 1024, "train_s": train_s,
+               "loss_per_epoch": [float(x) for x in losses], "auc_heldout_states": held_auc,
+               "colliding_state_fraction": float(1 - valid.float().mean())}
+
+
+def measure_learned(args, env, a, b, plain_out, stream, flush, dev, probes: int = 16):
+    """Learned block order on the same edges: verdict identity with the plain path, blocks checked
+    per edge, the predictor's inference cost and the edges/s of scoring plus checking."""
+    import torch
+
+    from vamp_gb300._lib import check, lib
+
+    torch.cuda.synchronize()
+    plain = plain_out.clone()
+    plain_blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)
+    check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
+                                         plain.data_ptr(), plain_blocks.data_ptr(), stream.cuda_stream))
+    m, info = train_predictor(env, dev)
+    out = torch.empty(N_EDGES, dtype=torch.uint8, device=dev)
+    blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)
+    scores = torch.empty((N_EDGES, probes), dtype=torch.float32, device=dev)
+
+    def score():
+        check(lib.vg_mlp_score_edges_device(m, a.data_ptr(), b.data_ptr(), N_EDGES, probes, scores.data_ptr(),
+                                            stream.cuda_stream))
+
+    def ordered():
+        check(lib.vg_validate_motions_scored_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
+                                                    scores.data_ptr(), probes, out.data_ptr(), blocks.data_ptr(),
+                                                    stream.cuda_stream))
+
+    for _ in range(max(args.warmup, 3)):
+        score()
+        ordered()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        score()
+        ev[i][1].record(stream)
+        ordered()
+        ev[i][2].record(stream)
+    torch.cuda.synchronize()
+    check(lib.vg_mlp_error(m))
+    score_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
+    check_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
+    pv, lv = plain.cpu().numpy(), out.cpu().numpy()
+    pb, lb = plain_blocks.cpu().numpy(), blocks.cpu().numpy()
+    coll = pv == 0
+    lib.vg_mlp_destroy(m)
+    rows = N_EDGES * probes
+    return {
+        "verdicts_identical": bool(np.array_equal(pv, lv)),
+        "edges_per_s": N_EDGES / ((score_ms + check_ms) / 1e3),
+        "ms_per_step": score_ms + check_ms,
+        "inference_ms": score_ms,
+        "inference": {"states_scored": rows, "probes_per_edge": probes,
+                      "tflops": rows * 2 * (16 * 256 + 256 * 256 + 256) / (score_ms / 1e3) / 1e12},
+        "ordered_check_ms": check_ms,
+        "blocks_per_edge": {"plain": float(pb.mean()), "learned": float(lb.mean())},
+        "blocks_per_colliding_edge": {"plain": float(pb[coll].mean()), "learned": float(lb[coll].mean())},
+        "checks_saved_per_edge": float((pb - lb).mean()) * 8,
+        "predictor": info,
+    }
 
 
 def run_gpu(args, world, rank, local):
@@ -298,6 +461,7 @@ def run_gpu(args, world, rank, local):
     kernel_ms = float(np.mean(step_ms))
     kernel_ms = max_over_ranks(world, kernel_ms)
     value = world * N_EDGES / (kernel_ms / 1e3)
+    learned = None if args.no_learned else measure_learned(args, env, a, b, out, stream, flush, dev)
 
     # end to end through the C ABI with host buffers
     pa = torch.empty(a_np.shape, dtype=torch.float32, pin_memory=True).numpy()
@@ -352,6 +516,8 @@ def run_gpu(args, world, rank, local):
                                 f"algorithmic FLOPs counted by the CPU oracle on 8192 of the edges, scaled"}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, a_np, b_np)
+    if learned is not None:
+        line["learned"] = learned
     print(json.dumps(line))
 
 
@@ -362,11 +528,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-order measurement")
     ap.add_argument("--schedule", type=int, default=1, help="GPU edge schedule: 1 warp per edge, 0 lane-block per edge")
+    ap.add_argument("--workload", default="edges", choices=["edges", "capt"],
+                    help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "capt":
+        run_capt(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

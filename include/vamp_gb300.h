@@ -41,6 +41,7 @@ extern "C" {
 #define VG_SQRT_EXACT 1 /* correctly rounded sqrt as the NEON build computes it (vector/neon.hh:520-523) */
 
 typedef struct vg_env vg_env;
+typedef struct vg_mlp vg_mlp;
 
 /* Message for the calling thread's last error ("" if none). */
 const char *vg_last_error(void);
@@ -145,6 +146,88 @@ int vg_validate_states(const char *robot, vg_env *env, const float *q, size_t n,
 int vg_validate_motions(
     const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution, uint8_t *out);
 int vg_sphere_fk(const char *robot, const float *q, size_t n, float *out);
+
+/* ------------------------------------------------------------------- tensor-core GEMM
+ * D[M][N] (fp32) = A[M][K] * B[N][K]^T with A, B row-major bf16 (device pointers), on the 5th-
+ * generation tensor cores (tcgen05, FP32 accumulation in tensor memory).  M % 128 == 0,
+ * 16 <= N <= 256 with N % 16 == 0, K % 16 == 0.  *err (device int) is set to 1 if a kernel gave
+ * up waiting for its MMAs.  The building block of the learned block ordering's MLP; no
+ * counterpart in the reference (which has no learned component). */
+int vg_gemm_bf16_device(const void *a, const void *b, float *d, int M, int N, int K, int *err, void *stream);
+
+/* ------------------------------------------------------------- learned block ordering
+ * None of these has a counterpart in the reference, which checks an edge's blocks in one fixed
+ * order (planning/validate.hh:40-66).  They change which blocks of an edge are checked first,
+ * never a verdict.
+ *
+ * A collision predictor for one robot: features sin(q_d), cos(q_d) (zero-padded to 16 or 32
+ * columns) -> 256 -> 256 -> 1 with ReLU, BF16 weights and activations, FP32 accumulation, FP32
+ * master weights.  Parameters, in order: W1 [256][kin], b1 [256], W2 [256][256], b2 [256],
+ * w3 [256], b3 [1] with kin = 16 for dim <= 8, 32 for dim <= 16 (dim up to 16). */
+vg_mlp *vg_mlp_create(int dim, uint64_t seed);
+void vg_mlp_destroy(vg_mlp *m);
+size_t vg_mlp_param_count(int dim);
+int vg_mlp_get_params(const vg_mlp *m, float *out); /* host buffer of vg_mlp_param_count floats */
+int vg_mlp_set_params(vg_mlp *m, const float *in);
+
+/* Adam training (lr, beta 0.9 / 0.999) on n labelled configurations (device q [n][dim],
+ * valid [n]: 1 = collision free, the exact checker's verdicts) for `epochs` passes in
+ * minibatches of `batch` rows (a multiple of 128); the mean binary cross-entropy of each epoch
+ * goes to losses[epochs] (host, may be NULL).  Synchronous. */
+int vg_mlp_train_device(vg_mlp *m, const float *q, const uint8_t *valid, size_t n, int epochs, int batch, float lr,
+                        float *losses, void *stream);
+
+/* One forward and backward pass on n <= 65536 labelled configurations without an update:
+ * gradients (host, vg_mlp_param_count floats, parameter order) of the mean loss, the loss, and
+ * the BF16 features the GEMMs saw (host [n][kin] as floats, may be NULL).  For gradient checks. */
+int vg_mlp_gradients(vg_mlp *m, const float *q, const uint8_t *valid, size_t n, float *grads, float *loss,
+                     float *features);
+
+/* Collision probability per configuration (device q [n][dim] -> p [n]): the training forward
+ * (separate GEMM launches) and the fused inference kernel (weights resident in shared memory). */
+int vg_mlp_predict_device(vg_mlp *m, const float *q, size_t n, float *p, void *stream);
+int vg_mlp_infer_device(vg_mlp *m, const float *q, size_t n, float *p, void *stream);
+
+/* Logits of `probes` (1..32) states per edge, the state at fraction (p + 0.5) / probes from a to
+ * b: scores [n][probes]. */
+int vg_mlp_score_edges_device(vg_mlp *m, const float *a, const float *b, size_t n, int probes, float *scores,
+                              void *stream);
+
+/* VG_OK, or VG_ERR_CUDA if a tensor-core kernel of m gave up waiting for its MMAs (synchronous). */
+int vg_mlp_error(vg_mlp *m);
+
+/* validate_motion verdicts (those of vg_validate_motions_device, bit for bit) with each edge's
+ * blocks checked in the order the scores rank them: block 0 first, then blocks by the largest
+ * score over their states (probe scores interpolated along the edge); blocks past the 64th follow
+ * in the reference's order.  scores [n][probes] (device), any collision score.  `blocks` gets the
+ * number of blocks checked.  Always the same-edge schedule. */
+int vg_validate_motions_scored_device(
+    const char *robot,
+    vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    const float *scores,
+    int probes,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream);
+
+/* Scores with m (vg_mlp_score_edges_device into m's scratch) and checks in learned order
+ * (vg_validate_motions_scored_device).  Calls sharing m must not overlap. */
+int vg_validate_motions_learned_device(
+    const char *robot,
+    vg_env *env,
+    vg_mlp *m,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    int probes,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream);
 
 /* Page-locked host memory for the host-buffer calls. */
 void *vg_host_alloc(size_t bytes);

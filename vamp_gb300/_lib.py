@@ -55,6 +55,20 @@ def _load() -> ctypes.CDLL:
         "vg_validate_states": ([_s, _p, _p, _sz, _p], _i),
         "vg_validate_motions": ([_s, _p, _p, _p, _sz, _i, _p], _i),
         "vg_sphere_fk": ([_s, _p, _sz, _p], _i),
+        "vg_gemm_bf16_device": ([_p, _p, _p, _i, _i, _i, _p, _p], _i),
+        "vg_mlp_create": ([_i, ctypes.c_uint64], _p),
+        "vg_mlp_destroy": ([_p], None),
+        "vg_mlp_param_count": ([_i], _sz),
+        "vg_mlp_get_params": ([_p, _p], _i),
+        "vg_mlp_set_params": ([_p, _p], _i),
+        "vg_mlp_train_device": ([_p, _p, _p, _sz, _i, _i, _f, _p, _p], _i),
+        "vg_mlp_gradients": ([_p, _p, _p, _sz, _p, _p, _p], _i),
+        "vg_mlp_predict_device": ([_p, _p, _sz, _p, _p], _i),
+        "vg_mlp_infer_device": ([_p, _p, _sz, _p, _p], _i),
+        "vg_mlp_score_edges_device": ([_p, _p, _p, _sz, _i, _p, _p], _i),
+        "vg_mlp_error": ([_p], _i),
+        "vg_validate_motions_scored_device": ([_s, _p, _p, _p, _sz, _i, _p, _i, _p, _p, _p], _i),
+        "vg_validate_motions_learned_device": ([_s, _p, _p, _p, _p, _sz, _i, _i, _p, _p, _p], _i),
         "vg_host_alloc": ([_sz], _p),
         "vg_host_free": ([_p], None),
     }
@@ -98,6 +112,20 @@ EXPORTED = (
     "vg_validate_states",
     "vg_validate_motions",
     "vg_sphere_fk",
+    "vg_gemm_bf16_device",
+    "vg_mlp_create",
+    "vg_mlp_destroy",
+    "vg_mlp_param_count",
+    "vg_mlp_get_params",
+    "vg_mlp_set_params",
+    "vg_mlp_train_device",
+    "vg_mlp_gradients",
+    "vg_mlp_predict_device",
+    "vg_mlp_infer_device",
+    "vg_mlp_score_edges_device",
+    "vg_mlp_error",
+    "vg_validate_motions_scored_device",
+    "vg_validate_motions_learned_device",
     "vg_host_alloc",
     "vg_host_free",
 )

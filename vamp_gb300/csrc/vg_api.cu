@@ -624,6 +624,49 @@ int vg_validate_motions_device(
     return VG_OK;
 }
 
+// Same verdicts as vg_validate_motions_device, with each edge's blocks checked in the order its
+// collision scores rank them (scores[e * probes + p]: any monotone collision score of the state at
+// fraction (p + 0.5) / probes along edge e, e.g. an MLP's logit).  The order is a permutation of
+// the edge's blocks, so the verdict is the AND over the same states; only the number of blocks
+// checked before a colliding edge stops (written to `blocks`) changes.  Always the same-edge
+// schedule.
+int vg_validate_motions_scored_device(
+    const char *robot,
+    vg_env *env,
+    const float *a,
+    const float *b,
+    size_t n,
+    int resolution,
+    const float *scores,
+    int probes,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!a || !b || !out || !scores)) || resolution < 1 || probes < 1 || probes > 32)
+        return set_error(VG_ERR_ARG, "vg_validate_motions_scored_device: bad argument (probes 1..32)");
+    if (n > 0x7fffffffu)
+        return set_error(VG_ERR_LIMIT, "vg_validate_motions_scored_device: more than 2^31 - 1 edges");
+    if (n == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int which = env->lanes == 8 ? 0 : 1;
+    int occ = 0;
+    if (int rc = prepare_kernel(r->edges_grouped_fn[which], smem, kBlock, &occ))
+        return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
+    const int per_block = kBlock / 32;
+    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
+    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env), scores, probes};
+    VG_CUDA(r->edges_grouped[which](p, grid, kBlock, smem, s), "edges kernel launch");
+    return VG_OK;
+}
+
 // For callers that must not allocate GPU memory while they run, e.g. a real-time planner that
 // reserves all memory up front so that no call can block on the allocator or fail for lack of
 // memory mid-plan, or a host framework that owns the device memory through its own pool.  Same

@@ -113,7 +113,64 @@ namespace vg
         int32_t *blocks;     // optional: blocks checked per edge
         unsigned *head;      // work counter, zero before launch
         EnvDevice env;
+        // learned order (same-edge schedule only): per-edge collision scores of `probes` states
+        // at fractions (p + 0.5) / probes along the edge; null = the reference's block order
+        const float *scores;
+        int probes;
     };
+
+    constexpr int kOrderMax = 64;  // blocks of an edge the learned order ranks; later ones follow in order
+
+    // Learned block order of one edge, written to order[0..min(n, kOrderMax)).  Block i holds the
+    // states at fractions (k n - i) / (W n), k = 1..W; its score is the largest probe score
+    // (linearly interpolated along the edge) over those states.  Block 0 stays first: it is the
+    // reference's first block and already ends most colliding edges.  Ties keep block order.
+    template <int W>
+    __device__ __forceinline__ void learned_order(const float *scores, int probes, int n, uint8_t *order)
+    {
+        const int lane = threadIdx.x & 31;
+        const float sp = lane < probes ? scores[lane] : 0.0f;
+        const int nb = n < kOrderMax ? n : kOrderMax;
+        const float inv = 1.0f / static_cast<float>(W * n);
+        float sc[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            const int i = lane + 32 * h;
+            float best = -INFINITY;
+#pragma unroll
+            for (int k = 1; k <= W; ++k)
+            {
+                float x = static_cast<float>(k * n - i) * inv * static_cast<float>(probes) - 0.5f;
+                x = fminf(fmaxf(x, 0.0f), static_cast<float>(probes - 1));
+                const int i0 = min(static_cast<int>(x), probes - 1);
+                const int i1 = min(i0 + 1, probes - 1);
+                const float s0 = __shfl_sync(0xffffffffu, sp, i0);
+                const float s1 = __shfl_sync(0xffffffffu, sp, i1);
+                best = fmaxf(best, fmaf(x - static_cast<float>(i0), s1 - s0, s0));
+            }
+            sc[h] = i == 0 ? INFINITY : (i < nb ? best : -INFINITY);
+        }
+        int rank[2] = {0, 0};
+        for (int j = 0; j < kOrderMax; ++j)
+        {
+            const float sj = __shfl_sync(0xffffffffu, sc[j >> 5], j & 31);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+                const int i = lane + 32 * h;
+                rank[h] += (sj > sc[h]) || (sj == sc[h] && j < i);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            const int i = lane + 32 * h;
+            if (i < nb)
+                order[rank[h]] = static_cast<uint8_t>(i);
+        }
+        __syncwarp();
+    }
 
     // |b - a| as the reference computes it on x86: squares summed lane-wise over the 8-wide
     // vectors that hold the configuration, then ((s0+s4)+(s2+s6)) + ((s1+s5)+(s3+s7)), then a
@@ -260,6 +317,7 @@ namespace vg
         const int sl = lane % W;
         const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
         constexpr unsigned kSegBits = W == 32 ? kFull : ((1u << W) - 1u);
+        __shared__ uint8_t s_order[4][kOrderMax];
 
         for (;;)
         {
@@ -292,19 +350,46 @@ namespace vg
             {
                 bs[d] = __fdiv_rn(v[d], denom);
             }
-            // segment `seg` starts at block `seg`
-            for (int k = 0; k < seg; ++k)
+            const bool learned = p.scores != nullptr && n > S;
+            uint8_t *order = s_order[threadIdx.x >> 5];
+            if (learned)
             {
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                {
-                    q[d] = __fsub_rn(q[d], bs[d]);
-                }
+                learned_order<W>(p.scores + static_cast<long long>(e) * p.probes, p.probes, n, order);
             }
+            // q holds block `cur`; block i is block 0 minus i repeated steps, as the reference
+            // computes it (planning/validate.hh:50-56)
+            int cur = 0;
             int verdict = 1, checked = n;
             for (int i0 = 0; i0 < n; i0 += S)
             {
-                const bool active = i0 + seg < n;
+                const int slot = i0 + seg;
+                const bool active = slot < n;
+                int want = slot;
+                if (learned && active && slot < kOrderMax)
+                {
+                    want = order[slot];
+                }
+                if (active)
+                {
+                    if (want < cur)
+                    {
+#pragma unroll
+                        for (int d = 0; d < D; ++d)
+                        {
+                            q[d] = __fmaf_rn(v[d], pct, p.a[static_cast<long long>(e) * D + d]);
+                        }
+                        cur = 0;
+                    }
+#pragma unroll 1
+                    for (; cur < want; ++cur)
+                    {
+#pragma unroll
+                        for (int d = 0; d < D; ++d)
+                        {
+                            q[d] = __fsub_rn(q[d], bs[d]);
+                        }
+                    }
+                }
                 const unsigned mask = __ballot_sync(kFull, active);
                 const unsigned alive = run_fkcc<Robot, W>(ev, q, mask);
                 const unsigned dead = mask & ~alive;
@@ -313,15 +398,6 @@ namespace vg
                     verdict = 0;
                     checked = i0 + (__ffs(dead) - 1) / W + 1;
                     break;
-                }
-#pragma unroll 1
-                for (int k = 0; k < S; ++k)
-                {
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                    {
-                        q[d] = __fsub_rn(q[d], bs[d]);
-                    }
                 }
             }
             (void)kSegBits;
