@@ -45,9 +45,16 @@ def sources() -> list[Path]:
 
 
 def _defines() -> list[str]:
-    # VG_MIN_BLOCKS: resident 128-thread blocks per SM the kernels are compiled for
+    # VG_MIN_BLOCKS: resident 128-thread blocks per SM the kernels are compiled for.
+    # VG_FORM_COMPACT=1: pass frames to the fine checks in registers instead of staging them in
+    # shared memory (the two schedule forms give identical results).
+    out = []
     mb = os.environ.get("VG_MIN_BLOCKS")
-    return [f"-DVG_MIN_BLOCKS={int(mb)}"] if mb else []
+    if mb:
+        out.append(f"-DVG_MIN_BLOCKS={int(mb)}")
+    if os.environ.get("VG_FORM_COMPACT") == "1":
+        out.append("-DVG_FORM_COMPACT")
+    return out
 
 
 def _compile(src: Path, verbose: bool) -> tuple[Path, str]:

@@ -574,7 +574,7 @@ int vg_validate_states_device(const char *robot, vg_env *env, const float *q, si
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
     int occ = 0;
     if (int rc = prepare_kernel(r->states_fn, smem, kBlock, &occ))
         return rc;
@@ -605,7 +605,7 @@ int vg_validate_motions_device(
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
     const int which = env->lanes == 8 ? 0 : 1;
     const bool grouped = env->schedule == 1;
     const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];
@@ -652,10 +652,10 @@ int vg_validate_motions_scored_device(
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
     const int which = env->lanes == 8 ? 0 : 1;
     int occ = 0;
-    if (int rc = prepare_kernel(r->edges_grouped_fn[which], smem, kBlock, &occ))
+    if (int rc = prepare_kernel(r->edges_learned_fn[which], smem, kBlock, &occ))
         return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
@@ -663,7 +663,7 @@ int vg_validate_motions_scored_device(
     const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
     const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
     EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env), scores, probes};
-    VG_CUDA(r->edges_grouped[which](p, grid, kBlock, smem, s), "edges kernel launch");
+    VG_CUDA(r->edges_learned[which](p, grid, kBlock, smem, s), "edges kernel launch");
     return VG_OK;
 }
 
@@ -703,7 +703,7 @@ int vg_validate_motions_device_noalloc(
         return rc;
     if (n == 0)
         return VG_OK;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4));
+    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
     const int which = env->lanes == 8 ? 0 : 1;
     const bool grouped = env->schedule == 1;
     const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];

@@ -532,6 +532,10 @@ namespace vg
         return __float_as_uint(__fmaf_rn(-rs, rs, sql2(ax, ay, az, bx, by, bz)));
     }
 
+    // Threads per block of every checking kernel, and the stride of the per-thread columns of
+    // the robots' shared-memory stage.
+    constexpr int kStageStride = 128;
+
     // The context a generated Robot::fkcc body runs against.
     template <int W>
     struct CheckCtx
@@ -542,6 +546,8 @@ namespace vg
         // every active lane's configuration lies inside the joint limits widened by the culling
         // slack: fine self pairs proven unable to collide there may be skipped
         bool in_limits = false;
+        // this thread's column of the robot's shared-memory stage: element i at stage[i * kStageStride]
+        float *stage = nullptr;
 
         __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
         {

@@ -28,6 +28,10 @@ namespace vg
         // same-edge schedule (a warp checks consecutive blocks of one edge)
         cudaError_t (*edges_grouped[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_grouped_fn[2];
+        // same-edge schedule in a learned block order (EdgesParams::scores)
+        cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_learned_fn[2];
+        int stage_floats;  // shared-memory staging floats per thread (after the environment image)
         cudaError_t (*spheres)(const float *, long long, float *, cudaStream_t);
     };
 

@@ -57,9 +57,9 @@ namespace vg
     }
 
     template <typename Robot, int W>
-    __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive)
+    __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
-        CheckCtx<W> ctx{ev, alive};
+        CheckCtx<W> ctx{ev, alive, false, stage};
         Robot::fkcc(q, ctx);
         return ctx.alive;
     }
@@ -79,6 +79,8 @@ namespace vg
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
+        // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
+        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
         constexpr int D = Robot::kDim;
         const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
         // every lane of a warp iterates the same number of times (warp-uniform loop)
@@ -93,7 +95,7 @@ namespace vg
             {
                 q[d] = in ? p.q[idx * D + d] : 0.0f;
             }
-            const unsigned alive = run_fkcc<Robot, 1>(ev, q, __ballot_sync(kFull, in));
+            const unsigned alive = run_fkcc<Robot, 1>(ev, q, __ballot_sync(kFull, in), stage);
             if (in)
             {
                 p.out[idx] = static_cast<uint8_t>((alive >> (threadIdx.x & 31)) & 1u);
@@ -121,16 +123,23 @@ namespace vg
 
     constexpr int kOrderMax = 64;  // blocks of an edge the learned order ranks; later ones follow in order
 
-    // Learned block order of one edge, written to order[0..min(n, kOrderMax)).  Block i holds the
-    // states at fractions (k n - i) / (W n), k = 1..W; its score is the largest probe score
-    // (linearly interpolated along the edge) over those states.  Block 0 stays first: it is the
-    // reference's first block and already ends most colliding edges.  Ties keep block order.
+    // Learned order of one edge's groups of S = 32 / W consecutive blocks (the blocks one warp
+    // iteration checks together, which keeps the warp's segments on neighbouring states), written
+    // to order[0..ceil(min(n, kOrderMax) / S)).  Block i holds the states at fractions
+    // (k n - i) / (W n), k = 1..W; its score is the largest probe score (linearly interpolated
+    // along the edge) over those states, and a group's score is its blocks' largest.  Group 0
+    // stays first: its block 0 is the reference's first block and already ends most colliding
+    // edges.  Ties keep the reference's order; any scores (NaN and infinities included) give a
+    // permutation of the groups.
     template <int W>
     __device__ __forceinline__ void learned_order(const float *scores, int probes, int n, uint8_t *order)
     {
+        constexpr int S = 32 / W;
+        constexpr int kGroups = kOrderMax / S;
         const int lane = threadIdx.x & 31;
         const float sp = lane < probes ? scores[lane] : 0.0f;
         const int nb = n < kOrderMax ? n : kOrderMax;
+        const int ng = (nb + S - 1) / S;
         const float inv = 1.0f / static_cast<float>(W * n);
         float sc[2];
 #pragma unroll
@@ -145,29 +154,40 @@ namespace vg
                 x = fminf(fmaxf(x, 0.0f), static_cast<float>(probes - 1));
                 const int i0 = min(static_cast<int>(x), probes - 1);
                 const int i1 = min(i0 + 1, probes - 1);
-                const float s0 = __shfl_sync(0xffffffffu, sp, i0);
-                const float s1 = __shfl_sync(0xffffffffu, sp, i1);
+                const float s0 = __shfl_sync(kFull, sp, i0);
+                const float s1 = __shfl_sync(kFull, sp, i1);
                 best = fmaxf(best, fmaf(x - static_cast<float>(i0), s1 - s0, s0));
             }
-            sc[h] = i == 0 ? INFINITY : (i < nb ? best : -INFINITY);
+            sc[h] = i < nb ? best : -INFINITY;
         }
-        int rank[2] = {0, 0};
-        for (int j = 0; j < kOrderMax; ++j)
-        {
-            const float sj = __shfl_sync(0xffffffffu, sc[j >> 5], j & 31);
+        // group g (lane g) = blocks g S .. g S + S - 1
+        float gs = -INFINITY;
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-            {
-                const int i = lane + 32 * h;
-                rank[h] += (sj > sc[h]) || (sj == sc[h] && j < i);
-            }
+        for (int j = 0; j < S; ++j)
+        {
+            const int i = (lane % kGroups) * S + j;
+            const float v0 = __shfl_sync(kFull, sc[0], i & 31);
+            const float v1 = __shfl_sync(kFull, sc[1], i & 31);
+            gs = fmaxf(gs, i < 32 ? v0 : v1);
         }
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
+        if (lane == 0)
         {
-            const int i = lane + 32 * h;
-            if (i < nb)
-                order[rank[h]] = static_cast<uint8_t>(i);
+            gs = INFINITY;
+        }
+        if (lane >= ng)
+        {
+            gs = -INFINITY;
+        }
+        int rank = 0;
+#pragma unroll 1
+        for (int j = 0; j < kGroups; ++j)
+        {
+            const float sj = __shfl_sync(kFull, gs, j);
+            rank += (sj > gs) || (sj == gs && j < lane);
+        }
+        if (lane < ng)
+        {
+            order[rank] = static_cast<uint8_t>(lane);
         }
         __syncwarp();
     }
@@ -200,6 +220,8 @@ namespace vg
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
+        // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
+        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
         constexpr int D = Robot::kDim;
         const int lane = threadIdx.x & 31;
         const int sl = lane % W;                  // lane within the segment
@@ -263,7 +285,7 @@ namespace vg
             {
                 break;
             }
-            const unsigned alive = run_fkcc<Robot, W>(ev, q, active);
+            const unsigned alive = run_fkcc<Robot, W>(ev, q, active, stage);
             bool finish = false;
             if (e >= 0)
             {
@@ -305,11 +327,13 @@ namespace vg
     // (block i = block 0 minus v / (W n), i times).  The edge is invalid if any checked block is,
     // and the reference would have stopped at the first invalid block, so the block count
     // reported is that block's index + 1.
-    template <typename Robot, int W>
+    template <typename Robot, int W, bool kLearned>
     __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_grouped_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
+        // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
+        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
         constexpr int D = Robot::kDim;
         constexpr int S = 32 / W;                 // segments (blocks) per warp
         const int lane = threadIdx.x & 31;
@@ -317,7 +341,8 @@ namespace vg
         const int sl = lane % W;
         const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
         constexpr unsigned kSegBits = W == 32 ? kFull : ((1u << W) - 1u);
-        __shared__ uint8_t s_order[4][kOrderMax];
+        constexpr unsigned kSegLeaders = W == 8 ? 0x01010101u : (W == 4 ? 0x11111111u : 1u);
+        __shared__ uint8_t s_order[kLearned ? 4 : 1][kOrderMax];
 
         for (;;)
         {
@@ -350,38 +375,86 @@ namespace vg
             {
                 bs[d] = __fdiv_rn(v[d], denom);
             }
-            const bool learned = p.scores != nullptr && n > S;
-            uint8_t *order = s_order[threadIdx.x >> 5];
-            if (learned)
-            {
-                learned_order<W>(p.scores + static_cast<long long>(e) * p.probes, p.probes, n, order);
-            }
             // q holds block `cur`; block i is block 0 minus i repeated steps, as the reference
             // computes it (planning/validate.hh:50-56)
             int cur = 0;
             int verdict = 1, checked = n;
-            for (int i0 = 0; i0 < n; i0 += S)
+            if constexpr (kLearned)
             {
-                const int slot = i0 + seg;
-                const bool active = slot < n;
-                int want = slot;
-                if (learned && active && slot < kOrderMax)
+                uint8_t *order = s_order[threadIdx.x >> 5];
+                const bool learned = n > S;
+                if (learned)
                 {
-                    want = order[slot];
+                    learned_order<W>(p.scores + static_cast<long long>(e) * p.probes, p.probes, n, order);
                 }
-                if (active)
+                constexpr int kGroups = kOrderMax / S;
+                int done = 0;  // blocks checked in earlier iterations
+                for (int i0 = 0; i0 < n; i0 += S)
                 {
-                    if (want < cur)
+                    const int g = i0 / S;
+                    const int want = (learned && g < kGroups ? static_cast<int>(order[g]) * S : i0) + seg;
+                    const bool active = want < n;
+                    if (active)
                     {
-#pragma unroll
-                        for (int d = 0; d < D; ++d)
+                        if (want < cur)
                         {
-                            q[d] = __fmaf_rn(v[d], pct, p.a[static_cast<long long>(e) * D + d]);
+#pragma unroll
+                            for (int d = 0; d < D; ++d)
+                            {
+                                q[d] = __fmaf_rn(v[d], pct, p.a[static_cast<long long>(e) * D + d]);
+                            }
+                            cur = 0;
                         }
-                        cur = 0;
+#pragma unroll 1
+                        for (; cur < want; ++cur)
+                        {
+#pragma unroll
+                            for (int d = 0; d < D; ++d)
+                            {
+                                q[d] = __fsub_rn(q[d], bs[d]);
+                            }
+                        }
+                    }
+                    const unsigned mask = __ballot_sync(kFull, active);
+                    const unsigned alive = run_fkcc<Robot, W>(ev, q, mask, stage);
+                    const unsigned dead = mask & ~alive;
+                    // one bit per active segment (its first lane)
+                    const unsigned leaders = mask & kSegLeaders;
+                    if (dead)
+                    {
+                        verdict = 0;
+                        const unsigned below = (1u << ((__ffs(dead) - 1) / W * W)) - 1u;
+                        checked = done + __popc(leaders & below) + 1;
+                        break;
+                    }
+                    done += __popc(leaders);
+                }
+            }
+            else
+            {
+                // segment `seg` starts at block `seg`
+                for (; cur < seg; ++cur)
+                {
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        q[d] = __fsub_rn(q[d], bs[d]);
+                    }
+                }
+                for (int i0 = 0; i0 < n; i0 += S)
+                {
+                    const bool active = i0 + seg < n;
+                    const unsigned mask = __ballot_sync(kFull, active);
+                    const unsigned alive = run_fkcc<Robot, W>(ev, q, mask, stage);
+                    const unsigned dead = mask & ~alive;
+                    if (dead)
+                    {
+                        verdict = 0;
+                        checked = i0 + (__ffs(dead) - 1) / W + 1;
+                        break;
                     }
 #pragma unroll 1
-                    for (; cur < want; ++cur)
+                    for (int k = 0; k < S; ++k)
                     {
 #pragma unroll
                         for (int d = 0; d < D; ++d)
@@ -389,15 +462,6 @@ namespace vg
                             q[d] = __fsub_rn(q[d], bs[d]);
                         }
                     }
-                }
-                const unsigned mask = __ballot_sync(kFull, active);
-                const unsigned alive = run_fkcc<Robot, W>(ev, q, mask);
-                const unsigned dead = mask & ~alive;
-                if (dead)
-                {
-                    verdict = 0;
-                    checked = i0 + (__ffs(dead) - 1) / W + 1;
-                    break;
                 }
             }
             (void)kSegBits;

@@ -20,10 +20,10 @@ namespace vg
         return cudaGetLastError();
     }
 
-    template <typename R, int W>
+    template <typename R, int W, bool kLearned>
     cudaError_t launch_edges_grouped(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        edges_grouped_kernel<R, W><<<grid, block, smem, s>>>(p);
+        edges_grouped_kernel<R, W, kLearned><<<grid, block, smem, s>>>(p);
         return cudaGetLastError();
     }
 
@@ -58,10 +58,15 @@ namespace vg
         o.edges[1] = &launch_edges<R, 4>;
         o.edges_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8>);
         o.edges_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4>);
-        o.edges_grouped[0] = &launch_edges_grouped<R, 8>;
-        o.edges_grouped[1] = &launch_edges_grouped<R, 4>;
-        o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8>);
-        o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4>);
+        o.edges_grouped[0] = &launch_edges_grouped<R, 8, false>;
+        o.edges_grouped[1] = &launch_edges_grouped<R, 4, false>;
+        o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false>);
+        o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false>);
+        o.edges_learned[0] = &launch_edges_grouped<R, 8, true>;
+        o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
+        o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);
+        o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true>);
+        o.stage_floats = R::kStage;
         o.spheres = &launch_spheres<R>;
         return o;
     }

@@ -408,6 +408,34 @@ def limits_code(model: dict, cull) -> list:
     return lines
 
 
+def staged_frames(model: dict, kin) -> dict:
+    """Frames the fine checks use, in first-use order: frame id -> stage index (>= 0), or
+    -1 - k for the k-th frame whose twelve values are all constants (the root)."""
+    slots, _ = slot_table(model)
+    em = Emitter("cuda", SNAP32)
+    fr = emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
+    order = []
+    for e in model["env_checks"]:
+        order.append(kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0])
+    for e in model["self_checks"]:
+        A, B = _pairs_ab(e)
+        order.append(kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0])
+        order.append(kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0])
+    out, n_var, n_const = {}, 0, 0
+    for fid in order:
+        if fid in out:
+            continue
+        R, t = fr[fid]
+        vals = [R[r][c] for r in range(3) for c in range(3)] + list(t)
+        if all(isinstance(v, float) for v in vals):
+            out[fid] = -1 - n_const
+            n_const += 1
+        else:
+            out[fid] = n_var
+            n_var += 1
+    return out
+
+
 def _pairs_ab(e):
     A, B = [], []
     for sa, sb in e["fine"]:
@@ -488,6 +516,14 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int2 {pre}LivePair[{max(1, len(live_pairs))}] = {{{', '.join('{%d, %d}' % p for p in live_pairs) or '{0, 0}'}}};")
         all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
+        if not tabled:
+            em1 = Emitter("cuda", SNAP32)
+            fr1 = emit_frames(kin, em1, "q", sc_fn=lambda x, s_, c: "")
+            fv1 = frame_values(kin, fr1)
+            cfs = sorted(((-1 - k, fid) for fid, k in staged_frames(model, kin).items() if k < 0))
+            cf1 = ", ".join("{" + ", ".join(lit32(v) for v in fv1[fidx[fid]]) + "}" for _, fid in cfs) or "{0}"
+            w(f"    // frames of the fine checks whose twelve values are constants (stage index -1 - k)")
+            w(f"    __constant__ float {pre}ConstFrame[{max(1, len(cfs))}][12] = {{{cf1}}};")
         w("")
 
     w("struct %s" % S)
@@ -497,6 +533,13 @@ def gen_cuda(model: dict) -> str:
     w("    static constexpr int kFine = %d;" % len(model["fine_spheres"]))
     w("    static constexpr int kSlots = %d;" % len(slots))
     w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
+    staged_ids = {} if tabled else staged_frames(model, kin)
+    w("    // floats of shared-memory staging per thread (frames of the fine checks)")
+    w("#ifdef VG_FORM_COMPACT")
+    w("    static constexpr int kStage = 0;")
+    w("#else")
+    w("    static constexpr int kStage = %d;" % (12 * sum(1 for v in staged_ids.values() if v >= 0)))
+    w("#endif")
     w("    static constexpr int kResolution = %d;" % model["resolution"])
     w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
     w("    static constexpr float kMaxRadius = %s;" % lit32(model["max_radius"]))
@@ -623,15 +666,20 @@ def gen_cuda(model: dict) -> str:
         w("}  // namespace vg::robots")
         return "\n".join(lines) + "\n"
 
-    # ---- compact schedule: frames in registers, per-check code unrolled, per-sphere and per-pair
-    # work in rolled loops over constant tables (keeps the kernel small enough for the
-    # instruction cache)
+    # ---- compact and staged schedules.  Both: frames in registers while the kinematics run,
+    # coarse link spheres queried together, per-check code unrolled, per-sphere and per-pair work
+    # in rolled loops over constant tables.  Compact passes the frames to those loops in
+    # registers; staged (the default) writes the frames the fine checks need to shared memory
+    # once, so that the call sites pass frame indices and the frames need no registers across
+    # the checks (smaller code for the instruction cache, fewer live registers).
     pre = f"k{S}"
+    cull = load_cull(name)
     em = Emitter("cuda", SNAP32)
     fr = frames_block(em)
-    body = list(em.lines)
-    body += limits_code(model, load_cull(name))
+    head = list(em.lines)
+    head += limits_code(model, cull)
     fvals = frame_values(kin, fr)
+    sid = staged_frames(model, kin)
 
     def frame_expr(fid):
         return "vg::Frame{{" + ", ".join(em.ref(v) for v in fvals[fidx[fid]]) + "}}"
@@ -646,34 +694,50 @@ def gen_cuda(model: dict) -> str:
         return list(em.lines), (x, y, z, lit32(r))
 
     # coarse spheres of every environment-checked link: queried together, reused by self checks
-    body.append(f"float4 cs[{n_env}];")
+    coarse = [f"float4 cs[{n_env}];"]
     for k, e in enumerate(model["env_checks"]):
         ls, (x, y, z, r) = centre(coarse_slot[e["link"]], "c")
-        body.append("{")
-        body += ["    " + l for l in ls]
-        body.append(f"    cs[{k}] = make_float4({x}, {y}, {z}, {r});  // {e['link']}")
-        body.append("}")
-    body.append(f"unsigned ch[{n_env}];")
+        coarse.append("{")
+        coarse += ["    " + l for l in ls]
+        coarse.append(f"    cs[{k}] = make_float4({x}, {y}, {z}, {r});  // {e['link']}")
+        coarse.append("}")
+    coarse.append(f"unsigned ch[{n_env}];")
     nb = -(-n_env // COARSE_BATCH)
     base = 0
     for bi in range(nb):
         size = n_env // nb + (1 if bi < n_env % nb else 0)
-        body.append(f"ctx.template env_many<{size}>(cs + {base}, ctx.alive, ch + {base});")
+        coarse.append(f"ctx.template env_many<{size}>(cs + {base}, ctx.alive, ch + {base});")
         base += size
-    for k, e in enumerate(model["env_checks"]):
-        fid = kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0]
-        for sidx in e["fine"]:
-            assert kin.sphere_in_frame(slots[sidx][0], slots[sidx][1])[0] == fid
-        body.append(f"// environment: {e['link']} ({len(e['fine'])} fine spheres)")
-        body.append("{")
-        body.append(f"    const unsigned need = ch[{k}] & ctx.alive;")
-        body.append(f"    if (need)")
-        body.append("    {")
-        body.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, {frame_expr(fid)}, {env_start[k]}, {env_start[k + 1]}, need);")
-        body.append("        if (hit && !(ctx.alive &= ~hit)) return;")
-        body.append("    }")
-        body.append("}")
-    cull = load_cull(name)
+
+    stage = []
+    for fid, k in sid.items():
+        if k < 0:
+            continue
+        vals = fvals[fidx[fid]]
+        stage.append(" ".join(f"st[{12 * k + j} * vg::kStageStride] = {em.ref(v)};" for j, v in enumerate(vals)) + f"  // {fid}")
+    const_frames = sorted(((-1 - k, fid) for fid, k in sid.items() if k < 0))
+
+    def env_section(staged):
+        out = []
+        for k, e in enumerate(model["env_checks"]):
+            fid = kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0]
+            for sidx in e["fine"]:
+                assert kin.sphere_in_frame(slots[sidx][0], slots[sidx][1])[0] == fid
+            fa = str(sid[fid]) if staged else frame_expr(fid)
+            out.append(f"// environment: {e['link']} ({len(e['fine'])} fine spheres)")
+            out.append("{")
+            out.append(f"    const unsigned need = ch[{k}] & ctx.alive;")
+            out.append(f"    if (need)")
+            out.append("    {")
+            if staged:
+                out.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, st, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
+            else:
+                out.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
+            out.append("        if (hit && !(ctx.alive &= ~hit)) return;")
+            out.append("    }")
+            out.append("}")
+        return out
+
     full_start, full_pairs, lv_start, lv_pairs = [0], [], [0], []
     for ci, e in enumerate(model["self_checks"]):
         full_pairs += [tuple(p_) for p_ in e["fine"]]
@@ -681,25 +745,37 @@ def gen_cuda(model: dict) -> str:
         sel = range(len(e["fine"])) if cull is None or cull["live"][ci] is None else cull["live"][ci]
         lv_pairs += [tuple(e["fine"][pi]) for pi in sel]
         lv_start.append(len(lv_pairs))
-    for ci, e in enumerate(model["self_checks"]):
-        a, b = e["links"]
-        A, B = _pairs_ab(e)
-        fa = kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0]
-        fb = kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0]
-        ka, kb = env_index[a], env_index[b]
-        nl = lv_start[ci + 1] - lv_start[ci]
-        body.append(f"// self: {a} vs. {b} ({nl} of {len(e['fine'])} fine pairs can collide inside the limits)")
-        body.append("{")
-        body.append(f"    const unsigned need = ctx.self_hit(cs[{ka}].x, cs[{ka}].y, cs[{ka}].z, cs[{ka}].w, cs[{kb}].x, cs[{kb}].y, cs[{kb}].z, cs[{kb}].w, ctx.alive);")
-        body.append("    if (need)")
-        body.append("    {")
-        body.append(f"        const unsigned acc = ctx.in_limits ? self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
-        body.append(f"                                           : self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
-        body.append("        const unsigned hit = ctx.vote(acc, need);")
-        body.append("        if (hit && !(ctx.alive &= ~hit)) return;")
-        body.append("    }")
-        body.append("}")
 
+    def self_section(staged):
+        out = []
+        for ci, e in enumerate(model["self_checks"]):
+            a, b = e["links"]
+            A, B = _pairs_ab(e)
+            fa = kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0]
+            fb = kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0]
+            ka, kb = env_index[a], env_index[b]
+            nl = lv_start[ci + 1] - lv_start[ci]
+            out.append(f"// self: {a} vs. {b} ({nl} of {len(e['fine'])} fine pairs can collide inside the limits)")
+            out.append("{")
+            out.append(f"    const unsigned need = ctx.self_hit(cs[{ka}].x, cs[{ka}].y, cs[{ka}].z, cs[{ka}].w, cs[{kb}].x, cs[{kb}].y, cs[{kb}].z, cs[{kb}].w, ctx.alive);")
+            out.append("    if (need)")
+            out.append("    {")
+            if staged:
+                out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
+                out.append(f"                                           : self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
+            else:
+                out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
+                out.append(f"                                           : self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
+            out.append("        const unsigned hit = ctx.vote(acc, need);")
+            out.append("        if (hit && !(ctx.alive &= ~hit)) return;")
+            out.append("    }")
+            out.append("}")
+        return out
+
+    compact_body = head + coarse + env_section(False) + self_section(False)
+    staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
+
+    w("#ifdef VG_FORM_COMPACT")
     w(f"""    // Fine environment tests of the spheres EnvFine[k0..k1) of one frame, for the segments in
     // `need`: the segments whose block collides.
     template <int W>
@@ -748,9 +824,87 @@ def gen_cuda(model: dict) -> str:
     w("    template <typename Ctx>")
     w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
     w("    {")
-    for l in body:
+    for l in compact_body:
         w("        " + l)
     w("    }")
+    w("#else")
+    w(f"""    // Frame f of this thread's stage (f >= 0), or constant frame -1 - f.
+    static __device__ __forceinline__ vg::Frame frame_at(const float *st, int f)
+    {{
+        vg::Frame r;
+        if (f >= 0)
+        {{
+#pragma unroll
+            for (int c = 0; c < 12; ++c)
+            {{
+                r.m[c] = st[(12 * f + c) * vg::kStageStride];
+            }}
+        }}
+        else
+        {{
+#pragma unroll
+            for (int c = 0; c < 12; ++c)
+            {{
+                r.m[c] = {pre}ConstFrame[-1 - f][c];
+            }}
+        }}
+        return r;
+    }}
+
+    // Fine environment tests of the spheres EnvFine[k0..k1) of staged frame f, for the segments
+    // in `need`: the segments whose block collides.
+    template <int W>
+    static __device__ __noinline__ unsigned env_fine(const vg::EnvView &ev, const float *st, int f, int k0, int k1, unsigned need)
+    {{
+        const vg::Frame fr = frame_at(st, f);
+        unsigned dead = 0u;
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k)
+        {{
+            const float4 o = {pre}SlotOff[{pre}EnvFine[k]];
+            const float4 c = vg::frame_point(fr, o);
+            const unsigned hit = vg::env_query_inline<W>(ev, c.x, c.y, c.z, c.w, need);
+            dead |= hit;
+            need &= ~hit;
+            if (!need)
+            {{
+                break;
+            }}
+        }}
+        return dead;
+    }}
+
+    // OR of the sign bits of the fine self-collision tests of pairs[k0..k1) (slot ids), the first
+    // slot of each pair in staged frame fa, the second in staged frame fb.
+    static __device__ __noinline__ unsigned self_pairs(const float *st, int fa, int fb, const int2 *pairs, int k0, int k1)
+    {{
+        const vg::Frame a = frame_at(st, fa), b = frame_at(st, fb);
+        unsigned acc = 0u;
+        int last = -1;
+        float4 ca = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k)
+        {{
+            const int2 pr = pairs[k];
+            if (pr.x != last)
+            {{
+                ca = vg::frame_point(a, {pre}SlotOff[pr.x]);
+                last = pr.x;
+            }}
+            const float4 cb = vg::frame_point(b, {pre}SlotOff[pr.y]);
+            acc |= vg::self_bits(ca.x, ca.y, ca.z, cb.x, cb.y, cb.z, __fadd_rn(ca.w, cb.w));
+        }}
+        return acc;
+    }}
+""")
+    w("    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.")
+    w("    template <typename Ctx>")
+    w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
+    w("    {")
+    for l in staged_body:
+        w("        " + l)
+    w("    }")
+    w("#endif")
     w("};")
     w("}  // namespace vg::robots")
     return "\n".join(lines) + "\n"
