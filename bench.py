@@ -370,7 +370,7 @@ def measure_learned(args, env, a, b, plain_out, stream, flush, dev, probes: int 
     plain_blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)
     check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
                                          plain.data_ptr(), plain_blocks.data_ptr(), stream.cuda_stream))
-    m, info = train_predictor(env, dev)
+    m, info = train_predictor(env, dev, n_labels=args.labels)
     out = torch.empty(N_EDGES, dtype=torch.uint8, device=dev)
     blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)
     scores = torch.empty((N_EDGES, probes), dtype=torch.float32, device=dev)
@@ -529,6 +529,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-order measurement")
+    ap.add_argument("--labels", type=int, default=2 << 20, help="exact-checker labels the learned order trains on")
     ap.add_argument("--schedule", type=int, default=1, help="GPU edge schedule: 1 warp per edge, 0 lane-block per edge")
     ap.add_argument("--workload", default="edges", choices=["edges", "capt"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload")

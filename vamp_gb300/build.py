@@ -47,13 +47,16 @@ def sources() -> list[Path]:
 def _defines() -> list[str]:
     # VG_MIN_BLOCKS: resident 128-thread blocks per SM the kernels are compiled for.
     # VG_FORM_COMPACT=1: pass frames to the fine checks in registers instead of staging them in
-    # shared memory (the two schedule forms give identical results).
+    # shared memory; VG_SELF_UNROLLED=1: one block of code per self-collision link pair instead
+    # of a loop over a table (all schedule forms give identical results).
     out = []
     mb = os.environ.get("VG_MIN_BLOCKS")
     if mb:
         out.append(f"-DVG_MIN_BLOCKS={int(mb)}")
     if os.environ.get("VG_FORM_COMPACT") == "1":
         out.append("-DVG_FORM_COMPACT")
+    if os.environ.get("VG_SELF_UNROLLED") == "1":
+        out.append("-DVG_SELF_UNROLLED")
     return out
 
 

@@ -524,6 +524,26 @@ def gen_cuda(model: dict) -> str:
             cf1 = ", ".join("{" + ", ".join(lit32(v) for v in fv1[fidx[fid]]) + "}" for _, fid in cfs) or "{0}"
             w(f"    // frames of the fine checks whose twelve values are constants (stage index -1 - k)")
             w(f"    __constant__ float {pre}ConstFrame[{max(1, len(cfs))}][12] = {{{cf1}}};")
+            sid1 = staged_frames(model, kin)
+            env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
+            rows_a, rows_b = [], []
+            lvs, fls, lv_n, fl_n = 0, 0, 0, 0
+            cull1 = load_cull(name)
+            for ci, e in enumerate(model["self_checks"]):
+                A, B = _pairs_ab(e)
+                fa = kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0]
+                fb = kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0]
+                sel = range(len(e["fine"])) if cull1 is None or cull1["live"][ci] is None else cull1["live"][ci]
+                nl, nf = len(list(sel)), len(e["fine"])
+                rows_a.append((env_ix[e["links"][0]], env_ix[e["links"][1]], sid1[fa], sid1[fb]))
+                rows_b.append((lvs, lvs + nl, fls, fls + nf))
+                lvs += nl
+                fls += nf
+            w(f"    // self-check loop: coarse sphere (env check index) of link A and B, their stage frames;")
+            w(f"    // live pair range, full pair range")
+            w(f"    __constant__ int4 {pre}SelfA[{len(rows_a)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_a)}}};")
+            w(f"    __constant__ int4 {pre}SelfB[{len(rows_b)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_b)}}};")
+            w(f"    __constant__ float {pre}CoarseR[{len(model['env_checks'])}] = {{{', '.join(lit32(model['coarse_spheres'][e['link']]['r']) for e in model['env_checks'])}}};")
         w("")
 
     w("struct %s" % S)
@@ -537,8 +557,12 @@ def gen_cuda(model: dict) -> str:
     w("    // floats of shared-memory staging per thread (frames of the fine checks)")
     w("#ifdef VG_FORM_COMPACT")
     w("    static constexpr int kStage = 0;")
+    n_stage_frames = sum(1 for v in staged_ids.values() if v >= 0)
+    w("#elif defined(VG_SELF_UNROLLED)")
+    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames))
     w("#else")
-    w("    static constexpr int kStage = %d;" % (12 * sum(1 for v in staged_ids.values() if v >= 0)))
+    w("    // and the coarse link spheres' centres (xyz), read by the self-check loop")
+    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + (0 if tabled else 3 * len(model["env_checks"]))))
     w("#endif")
     w("    static constexpr int kResolution = %d;" % model["resolution"])
     w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
@@ -773,7 +797,29 @@ def gen_cuda(model: dict) -> str:
         return out
 
     compact_body = head + coarse + env_section(False) + self_section(False)
+    c0 = 12 * sum(1 for v in sid.values() if v >= 0)
+    coarse_stage = [" ".join(f"st[{c0 + 3 * k + j} * vg::kStageStride] = cs[{k}].{'xyz'[j]};" for j in range(3))
+                    for k in range(n_env)]
+    self_loop = f"""#pragma unroll 1
+for (int c = 0; c < {len(model['self_checks'])}; ++c)
+{{
+    const int4 t = {pre}SelfA[c];
+    const float *ca = st + ({c0} + 3 * t.x) * vg::kStageStride;
+    const float *cb = st + ({c0} + 3 * t.y) * vg::kStageStride;
+    const unsigned need = ctx.self_hit(ca[0], ca[vg::kStageStride], ca[2 * vg::kStageStride], {pre}CoarseR[t.x],
+                                       cb[0], cb[vg::kStageStride], cb[2 * vg::kStageStride], {pre}CoarseR[t.y], ctx.alive);
+    if (need)
+    {{
+        const int4 u = {pre}SelfB[c];
+        const unsigned acc = ctx.in_limits ? self_pairs(st, t.z, t.w, {pre}LivePair, u.x, u.y)
+                                           : self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w);
+        const unsigned hit = ctx.vote(acc, need);
+        if (hit && !(ctx.alive &= ~hit)) return;
+    }}
+}}""".split("\n")
     staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
+    looped_body = (head + ["float *const st = ctx.stage;"] + stage + coarse + coarse_stage + env_section(True)
+                   + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
     w(f"""    // Fine environment tests of the spheres EnvFine[k0..k1) of one frame, for the segments in
@@ -901,8 +947,13 @@ def gen_cuda(model: dict) -> str:
     w("    template <typename Ctx>")
     w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
     w("    {")
+    w("#ifdef VG_SELF_UNROLLED")
     for l in staged_body:
         w("        " + l)
+    w("#else")
+    for l in looped_body:
+        w("        " + l)
+    w("#endif")
     w("    }")
     w("#endif")
     w("};")
