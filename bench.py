@@ -283,6 +283,111 @@ def run_capt(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup}))
 
 
+MIXED_ROBOTS = ("ur5", "fetch", "baxter", "panda")
+MIXED_EDGES = 16384
+
+
+def run_mixed(args, world, rank, local):
+    """Mixed-robot workload: UR5, Fetch, Baxter and Panda, 16,384 edges each (endpoints uniform
+    within each robot's limits, each robot's resolution), in the 60-primitive scene plus the
+    50,000-point surface cloud, one CAPT per robot built with its sphere radius range.  The four
+    checks run as one CUDA graph (vg_batch); the autotuner picks each robot's schedule first."""
+    import ctypes
+
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300._lib import check, lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    cloud = scenes.surface_pointcloud(SCENE_SEED, 50_000)
+    prims = scenes.scene_config1(SCENE_SEED)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    parts = []
+    for i, r in enumerate(MIXED_ROBOTS):
+        rb = getattr(vg, r)
+        r_min, r_max = rb.min_max_radii()
+        scene = dict(prims)
+        scene["pointclouds"] = [{"points": cloud, "r_min": r_min, "r_max": r_max, "r_point": scenes.POINT_RADIUS}]
+        env = vg.Environment.from_scene(scene)
+        a_np, b_np = scenes.edges(rb.s_m, rb.s_a, MIXED_EDGES, EDGE_SEED + 1 + i)
+        a, b = torch.from_numpy(a_np).to(dev), torch.from_numpy(b_np).to(dev)
+        out = torch.empty(MIXED_EDGES, dtype=torch.uint8, device=dev)
+        sched, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        check(lib.vg_autotune_motions(r.encode(), env.handle, a.data_ptr(), b.data_ptr(), 4096, rb.resolution(),
+                                      ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), s))
+        parts.append({"robot": r, "rb": rb, "env": env, "a": a, "b": b, "out": out,
+                      "pick": {"schedule": "warp per edge" if sched.value == 1 else "segment per edge",
+                               "blocks_per_sm": bps.value or "max", "sample_ms": ms.value}})
+
+    def timed(batch):
+        for _ in range(max(args.warmup, 3)):
+            check(lib.vg_batch_launch(batch, s))
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            check(lib.vg_batch_launch(batch, s))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    def make(sel, mlps=None, probes=8):
+        batch = lib.vg_batch_create()
+        for p in sel:
+            m = mlps[p["robot"]] if mlps else None
+            check(lib.vg_batch_add_motions(batch, p["robot"].encode(), p["env"].handle, p["a"].data_ptr(), p["b"].data_ptr(),
+                                           MIXED_EDGES, p["rb"].resolution(), m, probes if m else 0, p["out"].data_ptr(), None))
+        return batch
+
+    per_robot = {}
+    for p in parts:
+        bt = make([p])
+        ms = timed(bt)
+        lib.vg_batch_destroy(bt)
+        per_robot[p["robot"]] = {"edges_per_s": MIXED_EDGES / (ms / 1e3), "ms": ms, "resolution": p["rb"].resolution(),
+                                 "autotuner": p["pick"]}
+    alone = {p["robot"]: p["out"].cpu().numpy().copy() for p in parts}
+    bt = make(parts)
+    ms = timed(bt)
+    lib.vg_batch_destroy(bt)
+    identical = all(np.array_equal(alone[p["robot"]], p["out"].cpu().numpy()) for p in parts)
+    for p in parts:
+        per_robot[p["robot"]]["colliding_fraction"] = float(1 - p["out"].float().mean())
+    learned = None
+    if not args.no_learned:
+        mlps = {}
+        for p in parts:
+            q = torch.from_numpy(scenes.configurations(p["rb"].s_m, p["rb"].s_a, args.labels // 4, 300)).to(dev)
+            valid = torch.empty(len(q), dtype=torch.uint8, device=dev)
+            check(lib.vg_validate_states_device(p["robot"].encode(), p["env"].handle, q.data_ptr(), len(q), valid.data_ptr(), s))
+            m = lib.vg_mlp_create(p["rb"].dimension(), 5)
+            check(lib.vg_mlp_train_device(m, q.data_ptr(), valid.data_ptr(), len(q), 3, 1024, 1e-3, None, s))
+            mlps[p["robot"]] = m
+        bt = make(parts, mlps)
+        lms = timed(bt)
+        lib.vg_batch_destroy(bt)
+        learned = {"edges_per_s": len(parts) * MIXED_EDGES / (lms / 1e3), "ms": lms, "probes": 8,
+                   "labels_per_robot": args.labels // 4,
+                   "verdicts_identical": all(np.array_equal(alone[p["robot"]], p["out"].cpu().numpy()) for p in parts)}
+        for m in mlps.values():
+            lib.vg_mlp_destroy(m)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "edges validated/s on 1 GB300, mixed robots in one CUDA graph",
+            "value": len(parts) * MIXED_EDGES / (ms / 1e3), "unit": "edges/s", "ms_per_step": ms,
+            "workload": "ur5 + fetch + baxter + panda, 16384 edges each, 60 primitives + 50k-point CAPT per robot",
+            "verdicts_identical_to_single_checks": identical, "per_robot": per_robot, "learned": learned,
+            "steps": args.steps, "warmup": args.warmup, "l2": "flushed between timed steps (256 MB write)"}))
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -531,14 +636,17 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-order measurement")
     ap.add_argument("--labels", type=int, default=2 << 20, help="exact-checker labels the learned order trains on")
     ap.add_argument("--schedule", type=int, default=1, help="GPU edge schedule: 1 warp per edge, 0 lane-block per edge")
-    ap.add_argument("--workload", default="edges", choices=["edges", "capt"],
-                    help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload")
+    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed"],
+                    help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
+                         "mixed: four robots in one CUDA graph")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, world, rank)
     elif args.workload == "capt":
         run_capt(args, world, rank, local)
+    elif args.workload == "mixed":
+        run_mixed(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

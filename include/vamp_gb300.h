@@ -42,6 +42,7 @@ extern "C" {
 
 typedef struct vg_env vg_env;
 typedef struct vg_mlp vg_mlp;
+typedef struct vg_batch vg_batch;
 
 /* Message for the calling thread's last error ("" if none). */
 const char *vg_last_error(void);
@@ -228,6 +229,33 @@ int vg_validate_motions_learned_device(
     uint8_t *out,
     int32_t *blocks,
     void *stream);
+
+/* ------------------------------------------------------------- autotuning and batches
+ * Neither has a counterpart in the reference, which checks one edge per call on the calling
+ * thread (planning/validate.hh:24-77; callers rrtc.hh:136,176, prm.hh:122,138, fcit.hh:238,333).
+ *
+ * vg_autotune_motions times the edge-check schedules on the given edges (device buffers, a
+ * sample of the caller's workload) and keeps the fastest for this robot in env, where later edge
+ * checks of that robot use it: a segment or a warp per edge (*schedule_out 0 / 1) and the
+ * resident blocks per SM (*blocks_per_sm_out, 0 = as many as fit); *ms_out is its time on the
+ * sample.  Verdicts do not depend on the pick.  vg_env_set_schedule clears the picks.
+ * Synchronous. */
+int vg_autotune_motions(const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution,
+                        int *schedule_out, int *blocks_per_sm_out, float *ms_out, void *stream);
+
+/* A batch of edge checks (several robots, environments and edge sets; device buffers) run as
+ * one CUDA graph: vg_batch_launch captures the checks on its first call (and after a change to
+ * the batch or to one of its environments), one graph branch per check, and replays the graph
+ * on later calls, so a caller that refills the same buffers pays one launch per batch.  With
+ * mlp non-NULL a check scores `probes` states per edge with it and checks in learned order
+ * (vg_validate_motions_learned_device).  Verdicts equal vg_validate_motions_device's.  Calls on
+ * one batch must not overlap; the buffers must stay valid while the batch exists.  At most 64
+ * checks per batch. */
+vg_batch *vg_batch_create(void);
+void vg_batch_destroy(vg_batch *b);
+int vg_batch_add_motions(vg_batch *b, const char *robot, vg_env *env, const float *a, const float *goal, size_t n,
+                         int resolution, vg_mlp *mlp, int probes, uint8_t *out, int32_t *blocks);
+int vg_batch_launch(vg_batch *b, void *stream);
 
 /* Page-locked host memory for the host-buffer calls. */
 void *vg_host_alloc(size_t bytes);

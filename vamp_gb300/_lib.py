@@ -69,6 +69,11 @@ def _load() -> ctypes.CDLL:
         "vg_mlp_error": ([_p], _i),
         "vg_validate_motions_scored_device": ([_s, _p, _p, _p, _sz, _i, _p, _i, _p, _p, _p], _i),
         "vg_validate_motions_learned_device": ([_s, _p, _p, _p, _p, _sz, _i, _i, _p, _p, _p], _i),
+        "vg_autotune_motions": ([_s, _p, _p, _p, _sz, _i, _p, _p, _p, _p], _i),
+        "vg_batch_create": ([], _p),
+        "vg_batch_destroy": ([_p], None),
+        "vg_batch_add_motions": ([_p, _s, _p, _p, _p, _sz, _i, _p, _i, _p, _p], _i),
+        "vg_batch_launch": ([_p, _p], _i),
         "vg_host_alloc": ([_sz], _p),
         "vg_host_free": ([_p], None),
     }
@@ -126,6 +131,11 @@ EXPORTED = (
     "vg_mlp_error",
     "vg_validate_motions_scored_device",
     "vg_validate_motions_learned_device",
+    "vg_autotune_motions",
+    "vg_batch_create",
+    "vg_batch_destroy",
+    "vg_batch_add_motions",
+    "vg_batch_launch",
     "vg_host_alloc",
     "vg_host_free",
 )

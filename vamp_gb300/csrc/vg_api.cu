@@ -52,20 +52,10 @@ namespace vg
         return code;
     }
 
-    static int cuda_fail(cudaError_t e, const char *what)
+    int cuda_fail(cudaError_t e, const char *what)
     {
         return set_error(VG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     }
-
-#define VG_CUDA(call, what)                 \
-    do                                      \
-    {                                       \
-        const cudaError_t _e = (call);      \
-        if (_e != cudaSuccess)              \
-        {                                   \
-            return cuda_fail(_e, what);     \
-        }                                   \
-    } while (0)
 
     // ---------------------------------------------------------------- primitive bookkeeping
 
@@ -225,7 +215,7 @@ namespace vg
     }
 
     // Uploads the environment image if it changed; records the current device.
-    static int commit(vg_env *e)
+    int commit(vg_env *e)
     {
         int dev = 0;
         VG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
@@ -260,10 +250,11 @@ namespace vg
         e->image_f4 = img.size();
         e->device = dev;
         e->dirty = false;
+        ++e->version;
         return VG_OK;
     }
 
-    static EnvDevice env_device(const vg_env *e)
+    EnvDevice env_device(const vg_env *e)
     {
         EnvDevice d{};
         d.buf = e->d_image;
@@ -279,7 +270,7 @@ namespace vg
         return d;
     }
 
-    static int sm_count()
+    int sm_count()
     {
         static int count = 0;
         if (!count)
@@ -295,7 +286,7 @@ namespace vg
         return count;
     }
 
-    static int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm)
+    int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm)
     {
         if (smem > 48 * 1024)
         {
@@ -328,7 +319,45 @@ namespace vg
         return VG_OK;
     }
 
-    constexpr int kBlock = 128;
+    void tuned_for(const vg_env *env, const RobotOps *r, int *schedule, int *blocks_per_sm)
+    {
+        *schedule = env->schedule;
+        *blocks_per_sm = 0;
+        for (const RobotTune &t : env->tuned)
+        {
+            if (t.robot == r)
+            {
+                *schedule = t.schedule;
+                *blocks_per_sm = t.blocks_per_sm;
+            }
+        }
+    }
+
+    int launch_motions(const MotionLaunch &m, cudaStream_t s)
+    {
+        const RobotOps *r = m.r;
+        const vg_env *env = m.env;
+        const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
+        const int which = env->lanes == 8 ? 0 : 1;
+        const bool learned = m.scores != nullptr;
+        const bool grouped = learned || m.schedule == 1;
+        const void *fn = learned ? r->edges_learned_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]);
+        int occ = 0;
+        if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
+            return rc;
+        if (m.blocks_per_sm > 0 && m.blocks_per_sm < occ)
+            occ = m.blocks_per_sm;
+        VG_CUDA(cudaMemsetAsync(m.counter, 0, sizeof(unsigned), s), "reset work counter");
+        // edges handled at once by one block of threads: a warp each (same-edge schedule) or a
+        // segment each
+        const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
+        const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
+        const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+        EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes};
+        const auto launch = learned ? r->edges_learned[which] : (grouped ? r->edges_grouped[which] : r->edges[which]);
+        VG_CUDA(launch(p, grid, kBlock, smem, s), "edges kernel launch");
+        return VG_OK;
+    }
 
     // ------------------------------------------------------------ allocation-free variant
     //
@@ -543,6 +572,7 @@ int vg_env_set_schedule(vg_env *env, int schedule)
     if (!env || (schedule != 0 && schedule != 1))
         return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0 or 1");
     env->schedule = schedule;
+    env->tuned.clear();
     return VG_OK;
 }
 
@@ -605,23 +635,9 @@ int vg_validate_motions_device(
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    const int which = env->lanes == 8 ? 0 : 1;
-    const bool grouped = env->schedule == 1;
-    const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];
-    int occ = 0;
-    if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
-        return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
-    // edges handled at once by one block of threads: a warp each (same-edge schedule) or a
-    // segment each
-    const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
-    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
-    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
-    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env)};
-    VG_CUDA((grouped ? r->edges_grouped[which] : r->edges[which])(p, grid, kBlock, smem, s), "edges kernel launch");
-    return VG_OK;
+    MotionLaunch m{r, env, a, b, n, resolution, nullptr, 0, out, blocks, env->d_counter};
+    tuned_for(env, r, &m.schedule, &m.blocks_per_sm);
+    return launch_motions(m, static_cast<cudaStream_t>(stream));
 }
 
 // Same verdicts as vg_validate_motions_device, with each edge's blocks checked in the order its
@@ -652,19 +668,10 @@ int vg_validate_motions_scored_device(
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    const int which = env->lanes == 8 ? 0 : 1;
-    int occ = 0;
-    if (int rc = prepare_kernel(r->edges_learned_fn[which], smem, kBlock, &occ))
-        return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    VG_CUDA(cudaMemsetAsync(env->d_counter, 0, sizeof(unsigned), s), "reset work counter");
-    const int per_block = kBlock / 32;
-    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
-    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
-    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, env->d_counter, env_device(env), scores, probes};
-    VG_CUDA(r->edges_learned[which](p, grid, kBlock, smem, s), "edges kernel launch");
-    return VG_OK;
+    MotionLaunch m{r, env, a, b, n, resolution, scores, probes, out, blocks, env->d_counter};
+    int schedule = 1;
+    tuned_for(env, r, &schedule, &m.blocks_per_sm);
+    return launch_motions(m, static_cast<cudaStream_t>(stream));
 }
 
 // For callers that must not allocate GPU memory while they run, e.g. a real-time planner that
@@ -703,22 +710,9 @@ int vg_validate_motions_device_noalloc(
         return rc;
     if (n == 0)
         return VG_OK;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    const int which = env->lanes == 8 ? 0 : 1;
-    const bool grouped = env->schedule == 1;
-    const void *fn = grouped ? r->edges_grouped_fn[which] : r->edges_fn[which];
-    int occ = 0;
-    if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
-        return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    unsigned *counter = static_cast<unsigned *>(scratch);
-    VG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "clear scratch counter");
-    const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
-    const long long want = (static_cast<long long>(n) + per_block - 1) / per_block;
-    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
-    EdgesParams p{a, b, static_cast<int>(n), resolution, out, blocks, counter, env_device(env)};
-    VG_CUDA((grouped ? r->edges_grouped[which] : r->edges[which])(p, grid, kBlock, smem, s), "edges kernel launch");
-    return VG_OK;
+    MotionLaunch m{r, env, a, b, n, resolution, nullptr, 0, out, blocks, static_cast<unsigned *>(scratch)};
+    tuned_for(env, r, &m.schedule, &m.blocks_per_sm);
+    return launch_motions(m, static_cast<cudaStream_t>(stream));
 }
 
 int vg_sphere_fk_device(const char *robot, const float *q, size_t n, float *out, void *stream)

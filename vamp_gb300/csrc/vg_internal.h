@@ -40,6 +40,30 @@ namespace vg
 
     // thread-local last error message
     int set_error(int code, const std::string &msg);
+    int cuda_fail(cudaError_t e, const char *what);
+
+// return VG_ERR_CUDA (with the CUDA error in the message) from the enclosing function on failure
+#define VG_CUDA(call, what)                 \
+    do                                      \
+    {                                       \
+        const cudaError_t _e = (call);      \
+        if (_e != cudaSuccess)              \
+        {                                   \
+            return vg::cuda_fail(_e, what); \
+        }                                   \
+    } while (0)
+
+    // threads per block of every checking kernel (the robots' stage stride)
+    constexpr int kBlock = 128;
+    static_assert(kBlock == kStageStride, "stage columns are one per thread of a block");
+
+    // An autotuned schedule for one robot in one environment.
+    struct RobotTune
+    {
+        const RobotOps *robot;
+        int schedule;       // 0: a segment per edge, 1: a warp per edge
+        int blocks_per_sm;  // resident blocks per SM (0: as many as fit)
+    };
 }  // namespace vg
 
 // The C-ABI environment handle.
@@ -65,4 +89,37 @@ struct vg_env
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;
     size_t stage_cap = 0;
+    // per-robot picks of vg_autotune_motions (cleared by vg_env_set_schedule)
+    std::vector<vg::RobotTune> tuned;
+    // incremented by every upload of the image: CUDA graphs that captured an older image (its
+    // address and sizes) must be captured again
+    uint64_t version = 0;
 };
+
+namespace vg
+{
+    // One edge check, launched by launch_motions (the environment already on the device).
+    struct MotionLaunch
+    {
+        const RobotOps *r;
+        const vg_env *env;
+        const float *a;
+        const float *b;
+        size_t n;
+        int resolution;
+        const float *scores;  // non-null: learned block order (same-edge schedule)
+        int probes;
+        uint8_t *out;
+        int32_t *blocks;
+        unsigned *counter;     // work counter, cleared on the stream before the launch
+        int schedule = 1;      // 0: a segment per edge, 1: a warp per edge
+        int blocks_per_sm = 0;  // 0: as many as fit
+    };
+
+    int commit(vg_env *e);
+    EnvDevice env_device(const vg_env *e);
+    int sm_count();
+    int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm);
+    void tuned_for(const vg_env *env, const RobotOps *r, int *schedule, int *blocks_per_sm);
+    int launch_motions(const MotionLaunch &m, cudaStream_t s);
+}  // namespace vg
