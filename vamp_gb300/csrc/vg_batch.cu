@@ -34,6 +34,7 @@ struct vg_batch
     unsigned *counters = nullptr;  // one work counter per part (64 bytes apart)
     size_t counters_cap = 0;
     std::vector<float *> scores;   // per part with an MLP: [n][probes]
+    cudaStream_t capture = nullptr;  // the graph is captured here (the caller's stream may be the legacy default stream, which cannot be captured)
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> events;
     cudaGraph_t graph = nullptr;
@@ -88,6 +89,10 @@ namespace
             {
                 VG_CUDA(cudaMalloc(&bt->scores[i], p.n * p.probes * sizeof(float)), "cudaMalloc(batch scores)");
             }
+        }
+        if (!bt->capture)
+        {
+            VG_CUDA(cudaStreamCreateWithFlags(&bt->capture, cudaStreamNonBlocking), "cudaStreamCreate");
         }
         while (bt->side.size() < bt->parts.size())
         {
@@ -147,6 +152,8 @@ void vg_batch_destroy(vg_batch *b)
     for (float *p : b->scores)
         if (p)
             cudaFree(p);
+    if (b->capture)
+        cudaStreamDestroy(b->capture);
     for (cudaStream_t st : b->side)
         cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->events)
@@ -184,10 +191,10 @@ int vg_batch_launch(vg_batch *b, void *stream)
         if (int rc = prepare(b))
             return rc;
         // the capture records the launches without running them
-        VG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-        const int rc = record(b, s);
+        VG_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        const int rc = record(b, b->capture);
         cudaGraph_t g = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        const cudaError_t e = cudaStreamEndCapture(b->capture, &g);
         if (rc != VG_OK)
         {
             if (g)
