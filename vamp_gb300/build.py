@@ -48,7 +48,8 @@ def _defines() -> list[str]:
     # VG_MIN_BLOCKS: resident 128-thread blocks per SM the kernels are compiled for.
     # VG_FORM_COMPACT=1: pass frames to the fine checks in registers instead of staging them in
     # shared memory; VG_SELF_UNROLLED=1: one block of code per self-collision link pair instead
-    # of a loop over a table (all schedule forms give identical results).
+    # of a loop over a table; VG_STAGED_ALL=1: the staged form for the robots whose default is the
+    # table-driven form (all schedule forms give identical results).
     out = []
     mb = os.environ.get("VG_MIN_BLOCKS")
     if mb:
@@ -57,6 +58,8 @@ def _defines() -> list[str]:
         out.append("-DVG_FORM_COMPACT")
     if os.environ.get("VG_SELF_UNROLLED") == "1":
         out.append("-DVG_SELF_UNROLLED")
+    if os.environ.get("VG_STAGED_ALL") == "1":
+        out.append("-DVG_STAGED_ALL")
     return out
 
 

@@ -516,7 +516,7 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int2 {pre}LivePair[{max(1, len(live_pairs))}] = {{{', '.join('{%d, %d}' % p for p in live_pairs) or '{0, 0}'}}};")
         all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
-        if not tabled:
+        if True:
             em1 = Emitter("cuda", SNAP32)
             fr1 = emit_frames(kin, em1, "q", sc_fn=lambda x, s_, c: "")
             fv1 = frame_values(kin, fr1)
@@ -553,16 +553,16 @@ def gen_cuda(model: dict) -> str:
     w("    static constexpr int kFine = %d;" % len(model["fine_spheres"]))
     w("    static constexpr int kSlots = %d;" % len(slots))
     w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
-    staged_ids = {} if tabled else staged_frames(model, kin)
+    staged_ids = staged_frames(model, kin)
     w("    // floats of shared-memory staging per thread (frames of the fine checks)")
-    w("#ifdef VG_FORM_COMPACT")
+    w("#if defined(VG_FORM_COMPACT)%s" % (" || !defined(VG_STAGED_ALL)" if tabled else ""))
     w("    static constexpr int kStage = 0;")
     n_stage_frames = sum(1 for v in staged_ids.values() if v >= 0)
     w("#elif defined(VG_SELF_UNROLLED)")
     w("    static constexpr int kStage = %d;" % (12 * n_stage_frames))
     w("#else")
     w("    // and the coarse link spheres' centres (xyz), read by the self-check loop")
-    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + (0 if tabled else 3 * len(model["env_checks"]))))
+    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + 3 * len(model["env_checks"])))
     w("#endif")
     w("    static constexpr int kResolution = %d;" % model["resolution"])
     w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
@@ -589,6 +589,7 @@ def gen_cuda(model: dict) -> str:
     w("")
 
     if tabled:
+        w("#ifndef VG_STAGED_ALL")
         em = Emitter("cuda", SNAP32)
         fr = frames_block(em)
         body = list(em.lines)
@@ -686,9 +687,8 @@ def gen_cuda(model: dict) -> str:
             }}
         }}
     }}""")
-        w("};")
-        w("}  // namespace vg::robots")
-        return "\n".join(lines) + "\n"
+        w("#else")
+
 
     # ---- compact and staged schedules.  Both: frames in registers while the kinematics run,
     # coarse link spheres queried together, per-check code unrolled, per-sphere and per-pair work
@@ -956,6 +956,8 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
     w("#endif")
     w("    }")
     w("#endif")
+    if tabled:
+        w("#endif  // VG_STAGED_ALL")
     w("};")
     w("}  // namespace vg::robots")
     return "\n".join(lines) + "\n"
