@@ -333,13 +333,17 @@ namespace vg
         }
     }
 
-    // CAPT::collides_simd (collision/capt.hh:425-506) for one lane's sphere: true if the lane
-    // hits.  The reference's block result is the OR over its lanes; its early exits (no lane in
-    // the top box, no lane in its leaf box) return false for exactly the lanes that would not
-    // hit, so the per-lane form is the same test.
-    __device__ __forceinline__ bool capt_lane(const CaptView &c, float x, float y, float z, float r)
+    // CAPT::collides_simd (collision/capt.hh:425-506), per lane.  The reference's block result
+    // is the OR over its lanes; its early exits (no lane in the top box, no lane in its leaf box)
+    // return false for exactly the lanes that would not hit, so the per-lane form is the same
+    // test.  capt_locate does the box tests and the descent: the lane's sphere must be compared
+    // with the points of affordance blocks [b0, b1) (empty: it cannot hit), radius^2 rc.
+    __device__ __forceinline__ void capt_locate(const CaptView &c, float x, float y, float z, float r, uint32_t &b0,
+                                                uint32_t &b1, float &rc)
     {
+        b0 = b1 = 0;
         const float rad = __fadd_rn(r, c.r_point);
+        rc = __fmul_rn(rad, rad);
         const float p[3] = {x, y, z};
         bool in = true;
 #pragma unroll
@@ -349,7 +353,7 @@ namespace vg
         }
         if (!in)
         {
-            return false;
+            return;
         }
         int idx = 0;
         int k = 0;
@@ -371,34 +375,94 @@ namespace vg
             const float cl = m < hi ? m : hi;
             d[j] = __fsub_rn(p[j], cl);
         }
-        const float rc = __fmul_rn(rad, rad);
         if (!(__fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmul_rn(d[0], d[0]))) <= rc))
         {
-            return false;
+            return;
         }
-        const uint32_t b0 = __ldg(c.starts + leaf), b1 = __ldg(c.starts + leaf + 1);
-#pragma unroll 1
-        for (uint32_t b = b0; b < b1; ++b)
-        {
-            const float4 *blk = c.aff + 6 * static_cast<size_t>(b);
-            const float4 xs0 = __ldg(blk + 0), xs1 = __ldg(blk + 1), ys0 = __ldg(blk + 2), ys1 = __ldg(blk + 3);
-            const float4 zs0 = __ldg(blk + 4), zs1 = __ldg(blk + 5);
-            const float ax[8] = {xs0.x, xs0.y, xs0.z, xs0.w, xs1.x, xs1.y, xs1.z, xs1.w};
-            const float ay[8] = {ys0.x, ys0.y, ys0.z, ys0.w, ys1.x, ys1.y, ys1.z, ys1.w};
-            const float az[8] = {zs0.x, zs0.y, zs0.z, zs0.w, zs1.x, zs1.y, zs1.z, zs1.w};
-            bool hit = false;
+        b0 = __ldg(c.starts + leaf);
+        b1 = __ldg(c.starts + leaf + 1);
+    }
+
+    // Whether any of the 8 points of affordance block b lies within sqrt(rc) of (x, y, z).
+    __device__ __forceinline__ bool capt_block(const CaptView &c, uint32_t b, float x, float y, float z, float rc)
+    {
+        const float4 *blk = c.aff + 6 * static_cast<size_t>(b);
+        const float4 xs0 = __ldg(blk + 0), xs1 = __ldg(blk + 1), ys0 = __ldg(blk + 2), ys1 = __ldg(blk + 3);
+        const float4 zs0 = __ldg(blk + 4), zs1 = __ldg(blk + 5);
+        const float ax[8] = {xs0.x, xs0.y, xs0.z, xs0.w, xs1.x, xs1.y, xs1.z, xs1.w};
+        const float ay[8] = {ys0.x, ys0.y, ys0.z, ys0.w, ys1.x, ys1.y, ys1.z, ys1.w};
+        const float az[8] = {zs0.x, zs0.y, zs0.z, zs0.w, zs1.x, zs1.y, zs1.z, zs1.w};
+        bool hit = false;
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 8; ++j)
+        {
+            const float dx = __fsub_rn(ax[j], x), dy = __fsub_rn(ay[j], y), dz = __fsub_rn(az[j], z);
+            hit |= __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))) <= rc;
+        }
+        return hit;
+    }
+
+    // The CAPT query of every lane with `ask`, as a ballot of the lanes that hit.  Each lane's
+    // answer is the OR over the points of its affordance blocks, whoever scans them: when one
+    // lane's list is long compared with the warp's total (a tree built for large spheres affords
+    // thousands of points per leaf), the whole warp scans each lane's list in turn, 32 blocks at a
+    // time, instead of every lane walking its own.  Warp-uniform; all 32 lanes must call.
+    static __device__ __noinline__ unsigned capt_warp(const CaptView &c, float x, float y, float z, float r, bool ask)
+    {
+        const int lane = threadIdx.x & 31;
+        uint32_t b0 = 0, b1 = 0;
+        float rc = 0.0f;
+        if (ask)
+        {
+            capt_locate(c, x, y, z, r, b0, b1, rc);
+        }
+        const uint32_t len = b1 - b0;
+        const uint32_t longest = __reduce_max_sync(kFull, len);
+        if (longest == 0)
+        {
+            return 0u;
+        }
+        // warp iterations: each lane its own list (longest), or the lists one after another
+        const uint32_t shared_steps = __reduce_add_sync(kFull, (len + 31u) >> 5);
+        bool hit = false;
+        if (longest <= shared_steps)
+        {
+#pragma unroll 1
+            for (uint32_t b = b0; b < b1 && !hit; ++b)
             {
-                const float dx = __fsub_rn(ax[j], x), dy = __fsub_rn(ay[j], y), dz = __fsub_rn(az[j], z);
-                hit |= __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))) <= rc;
-            }
-            if (hit)
-            {
-                return true;
+                hit = capt_block(c, b, x, y, z, rc);
             }
         }
-        return false;
+        else
+        {
+            unsigned pending = __ballot_sync(kFull, len > 0);
+#pragma unroll 1
+            while (pending)
+            {
+                const int L = __ffs(pending) - 1;
+                pending &= pending - 1u;
+                const float qx = __shfl_sync(kFull, x, L), qy = __shfl_sync(kFull, y, L), qz = __shfl_sync(kFull, z, L);
+                const float qrc = __shfl_sync(kFull, rc, L);
+                const uint32_t s0 = __shfl_sync(kFull, b0, L), s1 = __shfl_sync(kFull, b1, L);
+                bool found = false;
+#pragma unroll 1
+                for (uint32_t base = s0; base < s1; base += 32u)
+                {
+                    const uint32_t b = base + static_cast<uint32_t>(lane);
+                    const bool h = b < s1 && capt_block(c, b, qx, qy, qz, qrc);
+                    if (__any_sync(kFull, h))
+                    {
+                        found = true;
+                        break;
+                    }
+                }
+                if (lane == L)
+                {
+                    hit = found;
+                }
+            }
+        }
+        return __ballot_sync(kFull, hit);
     }
 
     // sphere_environment_in_collision (validity.hh:47-150) for NS spheres at once, each over the
@@ -450,8 +514,7 @@ namespace vg
                 const bool ask = on && !((hit[s] >> lane) & 1u);
                 if (__any_sync(kFull, ask))
                 {
-                    const bool h = ask && capt_lane(e.clouds[c], x[s], y[s], z[s], r[s]);
-                    hit[s] |= seg_any<W>(__ballot_sync(kFull, h)) & mask;
+                    hit[s] |= seg_any<W>(capt_warp(e.clouds[c], x[s], y[s], z[s], r[s], ask)) & mask;
                 }
             }
         }
