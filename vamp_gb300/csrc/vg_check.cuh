@@ -407,7 +407,7 @@ namespace vg
     // lane's list is long compared with the warp's total (a tree built for large spheres affords
     // thousands of points per leaf), the whole warp scans each lane's list in turn, 32 blocks at a
     // time, instead of every lane walking its own.  Warp-uniform; all 32 lanes must call.
-    static __device__ __noinline__ unsigned capt_warp(const CaptView &c, float x, float y, float z, float r, bool ask)
+    __device__ __forceinline__ unsigned capt_warp(const CaptView &c, float x, float y, float z, float r, bool ask)
     {
         const int lane = threadIdx.x & 31;
         uint32_t b0 = 0, b1 = 0;
@@ -422,10 +422,11 @@ namespace vg
         {
             return 0u;
         }
-        // warp iterations: each lane its own list (longest), or the lists one after another
+        // warp iterations: each lane its own list (longest), or the lists one after another, 32
+        // blocks per step (a shared step costs about twice a lane step: broadcasts, votes)
         const uint32_t shared_steps = __reduce_add_sync(kFull, (len + 31u) >> 5);
         bool hit = false;
-        if (longest <= shared_steps)
+        if (longest <= 2u * shared_steps + 8u)
         {
 #pragma unroll 1
             for (uint32_t b = b0; b < b1 && !hit; ++b)

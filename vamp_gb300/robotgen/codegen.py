@@ -385,6 +385,46 @@ SNAP32 = 1e-7
 COARSE_BATCH = int(os.environ.get("VG_COARSE_BATCH", "6"))
 
 
+def f32_down(v: float) -> float:
+    """Largest float32 <= v (a conservative lower bound in FP32)."""
+    x = np.float32(v)
+    return float(x) if float(x) <= v else float(np.nextafter(x, np.float32(-np.inf)))
+
+
+def f32_up(v: float) -> float:
+    """Smallest float32 >= v."""
+    x = np.float32(v)
+    return float(x) if float(x) >= v else float(np.nextafter(x, np.float32(np.inf)))
+
+
+BIG = 3.0e38  # an unbounded box side (joint values are finite)
+
+
+def danger_boxes(model: dict, cull) -> tuple:
+    """Per self check ((joint indices, index of its first pair box or -1), union box) and the
+    boxes of the analysed checks' live pairs, as FP32 bounds rounded outwards; unanalysed checks
+    get an unbounded union box and no pair boxes."""
+    checks, pairs = [], []
+    for ci, e in enumerate(model["self_checks"]):
+        bx = None if cull is None or "boxes" not in cull else cull["boxes"][ci]
+        sel = range(len(e["fine"])) if cull is None or cull["live"][ci] is None else cull["live"][ci]
+        n_live = len(list(sel))
+        if not bx:
+            checks.append(((0, 0, -1), (-BIG, BIG, -BIG, BIG)))
+            continue
+        j = bx[0]["joints"]
+        two = len(j) == 2
+        jj = (j[0], j[1] if two else j[0])
+        per = []
+        for b in bx:
+            lo1, hi1 = (b["lo"][1], b["hi"][1]) if two else (-BIG, BIG)
+            per.append((f32_down(b["lo"][0]), f32_up(b["hi"][0]), f32_down(lo1) if two else -BIG, f32_up(hi1) if two else BIG))
+        union = (min(p[0] for p in per), max(p[1] for p in per), min(p[2] for p in per), max(p[3] for p in per))
+        checks.append(((jj[0], jj[1], len(pairs)), union))
+        pairs += per
+    return checks, pairs
+
+
 def load_cull(name: str):
     """Live fine self pairs per self check (None: all live), from robots/<name>.cull.json."""
     path = MODELS / f"{name}.cull.json"
@@ -498,13 +538,20 @@ def gen_cuda(model: dict) -> str:
             v = kin.sphere_in_frame(l, p)[1]
             offs.append(f"{{{lit32(em0.const(float(v[0])))}, {lit32(em0.const(float(v[1])))}, {lit32(em0.const(float(v[2])))}, {lit32(r)}}}")
         w(f"    __constant__ float4 {pre}SlotOff[{len(slots)}] = {{{', '.join(offs)}}};")
+        # tables of the table-driven form: only where that form is compiled
+        tab_if = "#ifndef VG_STAGED_ALL" if tabled else "#if 0"
+        stg_if = "#ifdef VG_STAGED_ALL" if tabled else "#if 1"
+        w(tab_if)
         w(f"    __constant__ int {pre}EnvCoarse[{len(model['env_checks'])}] = {{{', '.join(str(coarse_slot[e['link']]) for e in model['env_checks'])}}};")
         w(f"    __constant__ int {pre}EnvStart[{len(env_start)}] = {{{', '.join(map(str, env_start))}}};")
+        w("#endif")
         w(f"    __constant__ int {pre}EnvFine[{len(env_fine)}] = {{{', '.join(map(str, env_fine))}}};")
+        w(tab_if)
         w(f"    // per link pair: coarse slot A, coarse slot B, start of A's and B's fine lists, their sizes")
         w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
         w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
         w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
+        w("#endif")
         cull = load_cull(name)
         live_start, live_pairs = [0], []
         for ci, e in enumerate(model["self_checks"]):
@@ -515,6 +562,7 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int {pre}LiveStart[{len(live_start)}] = {{{', '.join(map(str, live_start))}}};")
         w(f"    __constant__ int2 {pre}LivePair[{max(1, len(live_pairs))}] = {{{', '.join('{%d, %d}' % p for p in live_pairs) or '{0, 0}'}}};")
         all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
+        w(stg_if)
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         if True:
             em1 = Emitter("cuda", SNAP32)
@@ -544,6 +592,16 @@ def gen_cuda(model: dict) -> str:
             w(f"    __constant__ int4 {pre}SelfA[{len(rows_a)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_a)}}};")
             w(f"    __constant__ int4 {pre}SelfB[{len(rows_b)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_b)}}};")
             w(f"    __constant__ float {pre}CoarseR[{len(model['env_checks'])}] = {{{', '.join(lit32(model['coarse_spheres'][e['link']]['r']) for e in model['env_checks'])}}};")
+            cb_checks, cb_pairs = danger_boxes(model, cull1)
+            box = lambda b: "{%s}" % ", ".join(lit32(v) for v in b)  # noqa: E731
+            w(f"    // danger boxes (joint space, inside the widened limits): a live pair can come within the")
+            w(f"    // culling margin only for joint values inside its box; per self check the two joints and")
+            w(f"    // the union of its pairs' boxes (and where its live pairs' boxes start, -1: none), per")
+            w(f"    // live pair of an analysed check its box (lo0, hi0, lo1, hi1)")
+            w(f"    __constant__ int4 {pre}SelfJoint[{len(cb_checks)}] = {{{', '.join('{%d, %d, %d, 0}' % c[0] for c in cb_checks)}}};")
+            w(f"    __constant__ float4 {pre}SelfBox[{len(cb_checks)}] = {{{', '.join(box(c[1]) for c in cb_checks)}}};")
+            w(f"    __constant__ float4 {pre}LiveBox[{max(1, len(cb_pairs))}] = {{{', '.join(box(p_) for p_ in cb_pairs) or box((0, 0, 0, 0))}}};")
+        w("#endif")
         w("")
 
     w("struct %s" % S)
@@ -561,8 +619,8 @@ def gen_cuda(model: dict) -> str:
     w("#elif defined(VG_SELF_UNROLLED)")
     w("    static constexpr int kStage = %d;" % (12 * n_stage_frames))
     w("#else")
-    w("    // and the coarse link spheres' centres (xyz), read by the self-check loop")
-    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + 3 * len(model["env_checks"])))
+    w("    // the coarse link spheres' centres (xyz) and the joint values, read by the self-check loop")
+    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + 3 * len(model["env_checks"]) + dim))
     w("#endif")
     w("    static constexpr int kResolution = %d;" % model["resolution"])
     w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
@@ -800,6 +858,8 @@ def gen_cuda(model: dict) -> str:
     c0 = 12 * sum(1 for v in sid.values() if v >= 0)
     coarse_stage = [" ".join(f"st[{c0 + 3 * k + j} * vg::kStageStride] = cs[{k}].{'xyz'[j]};" for j in range(3))
                     for k in range(n_env)]
+    qb = c0 + 3 * n_env
+    q_stage = [" ".join(f"st[{qb + d} * vg::kStageStride] = q[{d}];" for d in range(dim))]
     self_loop = f"""#pragma unroll 1
 for (int c = 0; c < {len(model['self_checks'])}; ++c)
 {{
@@ -811,14 +871,29 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
     if (need)
     {{
         const int4 u = {pre}SelfB[c];
-        const unsigned acc = ctx.in_limits ? self_pairs(st, t.z, t.w, {pre}LivePair, u.x, u.y)
-                                           : self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w);
+        unsigned acc = 0u;
+        if (ctx.in_limits)
+        {{
+            // live pairs only, and only while some lane's joints lie in the check's danger box
+            const int4 jj = {pre}SelfJoint[c];
+            const float4 bx = {pre}SelfBox[c];
+            const float qa = st[({qb} + jj.x) * vg::kStageStride], qb = st[({qb} + jj.y) * vg::kStageStride];
+            const bool in = (qa >= bx.x) & (qa <= bx.y) & (qb >= bx.z) & (qb <= bx.w);
+            if (__any_sync(vg::kFull, in))
+            {{
+                acc = self_pairs_boxed(st, t.z, t.w, u.x, u.y, jj.z, qa, qb);
+            }}
+        }}
+        else
+        {{
+            acc = self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w);
+        }}
         const unsigned hit = ctx.vote(acc, need);
         if (hit && !(ctx.alive &= ~hit)) return;
     }}
 }}""".split("\n")
     staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
-    looped_body = (head + ["float *const st = ctx.stage;"] + stage + coarse + coarse_stage + env_section(True)
+    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse + coarse_stage + env_section(True)
                    + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
@@ -932,6 +1007,40 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
         for (int k = k0; k < k1; ++k)
         {{
             const int2 pr = pairs[k];
+            if (pr.x != last)
+            {{
+                ca = vg::frame_point(a, {pre}SlotOff[pr.x]);
+                last = pr.x;
+            }}
+            const float4 cb = vg::frame_point(b, {pre}SlotOff[pr.y]);
+            acc |= vg::self_bits(ca.x, ca.y, ca.z, cb.x, cb.y, cb.z, __fadd_rn(ca.w, cb.w));
+        }}
+        return acc;
+    }}
+
+    // The same over the live pairs LivePair[k0..k1), skipping a pair when no lane's joint values
+    // (qa, qb: the check's two joints) lie in its danger box LiveBox[box0 + k - k0] (box0 < 0:
+    // the check has no boxes): outside it the pair keeps the culling margin, so its test value
+    // cannot be negative.  Warp-uniform; all 32 lanes call.
+    static __device__ __noinline__ unsigned self_pairs_boxed(const float *st, int fa, int fb, int k0, int k1, int box0,
+                                                             float qa, float qb)
+    {{
+        const vg::Frame a = frame_at(st, fa), b = frame_at(st, fb);
+        unsigned acc = 0u;
+        int last = -1;
+        float4 ca = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k)
+        {{
+            if (box0 >= 0)
+            {{
+                const float4 bx = {pre}LiveBox[box0 + k - k0];
+                if (!__any_sync(vg::kFull, (qa >= bx.x) & (qa <= bx.y) & (qb >= bx.z) & (qb <= bx.w)))
+                {{
+                    continue;
+                }}
+            }}
+            const int2 pr = {pre}LivePair[k];
             if (pr.x != last)
             {{
                 ca = vg::frame_point(a, {pre}SlotOff[pr.x]);

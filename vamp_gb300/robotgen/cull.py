@@ -86,9 +86,37 @@ def _moving_frame(model, link, p):
     return cur, (T @ np.array([*p, 1.0]))[:3]
 
 
-def analyse(model: dict) -> list:
+def _b_centres(model, down, qs, b_off) -> dict:
+    """World (A-frame) centres of the B spheres for the joint values qs [n, joints]."""
+    n = len(qs)
+    T = np.broadcast_to(np.eye(4), (n, 4, 4)).copy()
+    mi = 0
+    for j in down:
+        if j["type"] == "fixed":
+            T = T @ _tf(j)
+            continue
+        pre = np.eye(4)
+        pre[:3, :3] = rpy_matrix(j["rpy"])
+        pre[:3, 3] = j["xyz"]
+        T = T @ pre
+        w = np.asarray(j["axis"], float)
+        M = np.broadcast_to(np.eye(4), (n, 4, 4)).copy()
+        M[:, :3, :3] = _rot_batch(w / np.linalg.norm(w), qs[:, mi])
+        T = T @ M
+        mi += 1
+    return {sb: np.einsum("nij,j->ni", T, np.array([*off, 1.0]))[:, :3] for sb, off in b_off.items()}
+
+
+def analyse(model: dict, boxes: list | None = None) -> list:
     """For each self check, the indices (into its fine pair list) of pairs that may collide
-    inside the widened limits; None when the check was not analysed (all pairs kept)."""
+    inside the widened limits; None when the check was not analysed (all pairs kept).
+
+    With `boxes` (a list), also appends per self check either None or, per live pair, its
+    danger box: (joint indices, [lo, hi] per joint) containing every configuration inside the
+    widened limits at which the pair may come within MARGIN.  Outside the box the pair keeps
+    MARGIN clearance, by the same grid-plus-Lipschitz bound: a configuration with distance
+    <= MARGIN has a grid point within half a step per joint whose distance is <= MARGIN plus the
+    bound's slack, and the box covers every such grid point's cell."""
     names = model["joint_names"]
     lo = np.array(model["s_a"], float) - SLACK_RAD
     hi = np.array(model["s_a"], float) + np.array(model["s_m"], float) + SLACK_RAD
@@ -100,16 +128,22 @@ def analyse(model: dict) -> list:
         fb = {_moving_frame(model, fine[sb]["link"], fine[sb]["p"])[0] for _, sb in pairs}
         if len(fa) != 1 or len(fb) != 1:
             out.append(None)
+            if boxes is not None:
+                boxes.append(None)
             continue
         fa, fb = fa.pop(), fb.pop()
         ca, cb = _chain(model, fa), _chain(model, fb)
         if [j["name"] for j in cb[: len(ca)]] != [j["name"] for j in ca]:
             out.append(None)  # analysed only when A's frame is an ancestor of B's frame
+            if boxes is not None:
+                boxes.append(None)
             continue
         down = cb[len(ca):]
         moving = [j for j in down if j["type"] != "fixed"]
         if not moving or len(moving) > MAX_JOINTS or any(j["name"] not in names for j in moving):
             out.append(None)
+            if boxes is not None:
+                boxes.append(None)
             continue
         idx = [names.index(j["name"]) for j in moving]
         grids, steps = [], []
@@ -123,6 +157,7 @@ def analyse(model: dict) -> list:
         b_off = {sb: _moving_frame(model, fine[sb]["link"], fine[sb]["p"])[1] for sb in b_ids}
         mins = np.full(len(pairs), np.inf)
         dmax = np.zeros((len(b_ids), len(idx)))
+
         CH = 50000
         for s in range(0, len(mesh), CH):
             qs = mesh[s : s + CH]
@@ -167,6 +202,29 @@ def analyse(model: dict) -> list:
             if not (bound > MARGIN):
                 live.append(pi)
         out.append(live)
+        if boxes is not None:
+            # second pass: the grid points near enough to matter, per live pair
+            slack = {pi: sum(dmax[b_ids.index(pairs[pi][1]), k] * 1.01 * steps[k] / 2 for k in range(len(idx)))
+                     for pi in live}
+            blo = {pi: np.full(len(idx), np.inf) for pi in live}
+            bhi = {pi: np.full(len(idx), -np.inf) for pi in live}
+            for s0 in range(0, len(mesh), CH):
+                qs = mesh[s0 : s0 + CH]
+                bc = _b_centres(model, down, qs, b_off)
+                for pi in live:
+                    sa, sb = pairs[pi]
+                    pa, ra = a_pts[sa]
+                    d = np.linalg.norm(bc[sb] - pa, axis=1) - (ra + fine[sb]["r"])
+                    near = qs[d - slack[pi] <= MARGIN]
+                    if len(near):
+                        blo[pi] = np.minimum(blo[pi], near.min(0))
+                        bhi[pi] = np.maximum(bhi[pi], near.max(0))
+            per = []
+            for pi in live:
+                # one whole grid step of padding on each side (half a step covers the cells)
+                per.append({"joints": idx, "lo": [float(blo[pi][k] - steps[k]) for k in range(len(idx))],
+                            "hi": [float(bhi[pi][k] + steps[k]) for k in range(len(idx))]})
+            boxes.append(per)
     return out
 
 
@@ -181,8 +239,10 @@ def main():
     ap.add_argument("robots", nargs="*", default=["panda", "ur5", "fetch", "baxter"])
     a = ap.parse_args()
     for r in a.robots:
-        live = analyse(model(r))
-        out = {"slack_rad": SLACK_RAD, "margin": MARGIN, "step_rad": STEP_RAD, "max_joints": MAX_JOINTS, "live": live}
+        boxes = []
+        live = analyse(model(r), boxes)
+        out = {"slack_rad": SLACK_RAD, "margin": MARGIN, "step_rad": STEP_RAD, "max_joints": MAX_JOINTS, "live": live,
+               "boxes": boxes}
         Path(HERE / f"{r}.cull.json").write_text(json.dumps(out) + "\n")
         kept = sum(len(c["fine"]) if l is None else len(l) for c, l in zip(model(r)["self_checks"], live))
         total = sum(len(c["fine"]) for c in model(r)["self_checks"])
