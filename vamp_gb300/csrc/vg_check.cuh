@@ -333,6 +333,10 @@ namespace vg
         }
     }
 
+#ifndef VG_CAPT_SHARED_WEIGHT
+#define VG_CAPT_SHARED_WEIGHT 4
+#endif
+
     // CAPT::collides_simd (collision/capt.hh:425-506), per lane.  The reference's block result
     // is the OR over its lanes; its early exits (no lane in the top box, no lane in its leaf box)
     // return false for exactly the lanes that would not hit, so the per-lane form is the same
@@ -407,7 +411,7 @@ namespace vg
     // lane's list is long compared with the warp's total (a tree built for large spheres affords
     // thousands of points per leaf), the whole warp scans each lane's list in turn, 32 blocks at a
     // time, instead of every lane walking its own.  Warp-uniform; all 32 lanes must call.
-    __device__ __forceinline__ unsigned capt_warp(const CaptView &c, float x, float y, float z, float r, bool ask)
+    static __device__ __noinline__ unsigned capt_warp(const CaptView &c, float x, float y, float z, float r, bool ask)
     {
         const int lane = threadIdx.x & 31;
         uint32_t b0 = 0, b1 = 0;
@@ -423,10 +427,11 @@ namespace vg
             return 0u;
         }
         // warp iterations: each lane its own list (longest), or the lists one after another, 32
-        // blocks per step (a shared step costs about twice a lane step: broadcasts, votes)
+        // blocks per step (a shared step also pays broadcasts and a vote: weighted by
+        // VG_CAPT_SHARED_WEIGHT / 4)
         const uint32_t shared_steps = __reduce_add_sync(kFull, (len + 31u) >> 5);
         bool hit = false;
-        if (longest <= 2u * shared_steps + 8u)
+        if (4u * longest <= VG_CAPT_SHARED_WEIGHT * shared_steps)
         {
 #pragma unroll 1
             for (uint32_t b = b0; b < b1 && !hit; ++b)
