@@ -192,9 +192,6 @@ namespace vg
         return VG_OK;
     }
 
-    // mean affordance blocks per leaf above which the warp-cooperative scan is used
-    constexpr size_t kLongListBlocks = 48;
-
     static void pack_clouds(const vg_env *e, std::vector<float4> &img, int *cloud_off)
     {
         *cloud_off = static_cast<int>(img.size());
@@ -211,8 +208,6 @@ namespace vg
             v.r_point = c.r_point;
             v.nlog2 = c.nlog2;
             v.n_tests = static_cast<int>(c.tests.size());
-            // a warp shares the scan of long affordance lists (trees built for large spheres)
-            v.long_lists = c.blocks() > kLongListBlocks * (c.aff_starts.size() - 1) ? 1 : 0;
             const size_t at = img.size();
             img.resize(at + sizeof(CaptView) / sizeof(float4));
             std::memcpy(&img[at], &v, sizeof(CaptView));

@@ -179,8 +179,7 @@ namespace vg
         float r_point;
         int nlog2;
         int n_tests;
-        int long_lists;  // 1: leaves afford many blocks on average (warp-cooperative scan pays)
-        int pad[2];
+        int pad[3];
     };
     constexpr int kMaxClouds = 4;
 
@@ -407,23 +406,6 @@ namespace vg
         return hit;
     }
 
-    // The CAPT query of one lane, scanning its own list (short lists).
-    __device__ __forceinline__ bool capt_lane(const CaptView &c, float x, float y, float z, float r)
-    {
-        uint32_t b0, b1;
-        float rc;
-        capt_locate(c, x, y, z, r, b0, b1, rc);
-#pragma unroll 1
-        for (uint32_t b = b0; b < b1; ++b)
-        {
-            if (capt_block(c, b, x, y, z, rc))
-            {
-                return true;
-            }
-        }
-        return false;
-    }
-
     // The CAPT query of every lane with `ask`, as a ballot of the lanes that hit.  Each lane's
     // answer is the OR over the points of its affordance blocks, whoever scans them: when one
     // lane's list is long compared with the warp's total (a tree built for large spheres affords
@@ -538,10 +520,7 @@ namespace vg
                 const bool ask = on && !((hit[s] >> lane) & 1u);
                 if (__any_sync(kFull, ask))
                 {
-                    const unsigned h = e.clouds[c].long_lists
-                                           ? capt_warp(e.clouds[c], x[s], y[s], z[s], r[s], ask)
-                                           : __ballot_sync(kFull, ask && capt_lane(e.clouds[c], x[s], y[s], z[s], r[s]));
-                    hit[s] |= seg_any<W>(h) & mask;
+                    hit[s] |= seg_any<W>(capt_warp(e.clouds[c], x[s], y[s], z[s], r[s], ask)) & mask;
                 }
             }
         }
