@@ -337,7 +337,7 @@ namespace vg
     {
         const RobotOps *r = m.r;
         const vg_env *env = m.env;
-        const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
+        const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
         const int which = env->lanes == 8 ? 0 : 1;
         const bool learned = m.scores != nullptr;
         const bool grouped = learned || m.schedule == 1;
@@ -604,7 +604,7 @@ int vg_validate_states_device(const char *robot, vg_env *env, const float *q, si
         return VG_OK;
     if (int rc = commit(env))
         return rc;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
+    const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
     int occ = 0;
     if (int rc = prepare_kernel(r->states_fn, smem, kBlock, &occ))
         return rc;

@@ -235,7 +235,7 @@ int vg_autotune_motions(const char *robot, vg_env *env, const float *a, const fl
     int best_s = 1, best_b = 0, rc = VG_OK;
     float best = 1e30f;
     const int which = env->lanes == 8 ? 0 : 1;
-    const int smem = static_cast<int>(env->image_f4 * sizeof(float4)) + r->stage_floats * kBlock * 4;
+    const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
     for (int sched = 0; sched < 2 && rc == VG_OK; ++sched)
     {
         int occ = 0;

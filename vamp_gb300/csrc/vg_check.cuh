@@ -146,7 +146,7 @@ namespace vg
         const int E = static_cast<int>(u >> 23) - 127;
         const int odd = E & 1;
         const int k = (E - odd) >> 1;
-        const unsigned tb = tab[(static_cast<unsigned>(odd) << 10) | ((u >> 13) & 1023u)];
+        const unsigned tb = __ldg(tab + ((static_cast<unsigned>(odd) << 10) | ((u >> 13) & 1023u)));
         return __uint_as_float((static_cast<unsigned>(static_cast<int>(tb >> 23) - k) << 23) | (tb & 0x7fffffu));
     }
 

@@ -36,21 +36,30 @@ namespace vg
 
     constexpr int kRsqrtF4 = 2048 / 4;
 
+    // Float4s of the image each block stages into shared memory: all but the RSQRTPS table,
+    // which stays in global memory (read through the L1 cache), so that shared memory goes to
+    // more resident warps.
+    __host__ __device__ constexpr int staged_f4(int n_f4)
+    {
+        return n_f4 - kRsqrtF4;
+    }
+
     __device__ __forceinline__ EnvView stage_env(const EnvDevice &d, float4 *smem)
     {
-        for (int i = threadIdx.x; i < d.n_f4; i += blockDim.x)
+        const int n = staged_f4(d.n_f4);
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
         {
-            smem[i] = d.buf[i];
+            smem[i] = d.buf[kRsqrtF4 + i];
         }
         __syncthreads();
         EnvView v;
-        v.rsqrt_tab = reinterpret_cast<const uint32_t *>(smem);
+        v.rsqrt_tab = reinterpret_cast<const uint32_t *>(d.buf);
         v.sqrt_mode = d.sqrt_mode;
-        v.clouds = reinterpret_cast<const CaptView *>(smem + d.cloud_off);
+        v.clouds = reinterpret_cast<const CaptView *>(smem + d.cloud_off - kRsqrtF4);
         v.n_clouds = d.n_clouds;
         for (int k = 0; k < 5; ++k)
         {
-            v.rec[k] = smem + d.off[k];
+            v.rec[k] = smem + d.off[k] - kRsqrtF4;
             v.n[k] = d.n[k];
         }
         return v;
@@ -80,7 +89,7 @@ namespace vg
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
         // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
-        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
+        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
         constexpr int D = Robot::kDim;
         const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
         // every lane of a warp iterates the same number of times (warp-uniform loop)
@@ -221,7 +230,7 @@ namespace vg
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
         // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
-        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
+        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
         constexpr int D = Robot::kDim;
         const int lane = threadIdx.x & 31;
         const int sl = lane % W;                  // lane within the segment
@@ -333,7 +342,7 @@ namespace vg
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
         // this thread's column of the robot's shared-memory stage (blocks of kStageStride threads)
-        float *const stage = reinterpret_cast<float *>(smem + p.env.n_f4) + threadIdx.x;
+        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
         constexpr int D = Robot::kDim;
         constexpr int S = 32 / W;                 // segments (blocks) per warp
         const int lane = threadIdx.x & 31;

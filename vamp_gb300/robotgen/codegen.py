@@ -448,9 +448,10 @@ def limits_code(model: dict, cull) -> list:
     return lines
 
 
-def staged_frames(model: dict, kin) -> dict:
-    """Frames the fine checks use, in first-use order: frame id -> stage index (>= 0), or
-    -1 - k for the k-th frame whose twelve values are all constants (the root)."""
+def stage_layout(model: dict, kin, cull) -> dict:
+    """The staged form's shared-memory stage, per thread: the non-constant entries of the frames
+    the fine checks use (in first-use order), then the centres of the coarse spheres the self
+    loop reads, then the joint values the danger boxes test."""
     slots, _ = slot_table(model)
     em = Emitter("cuda", SNAP32)
     fr = emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
@@ -461,19 +462,31 @@ def staged_frames(model: dict, kin) -> dict:
         A, B = _pairs_ab(e)
         order.append(kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0])
         order.append(kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0])
-    out, n_var, n_const = {}, 0, 0
+    frames, fslots, fconsts, n = {}, [], [], 0
     for fid in order:
-        if fid in out:
+        if fid in frames:
             continue
+        frames[fid] = len(fslots)
         R, t = fr[fid]
-        vals = [R[r][c] for r in range(3) for c in range(3)] + list(t)
-        if all(isinstance(v, float) for v in vals):
-            out[fid] = -1 - n_const
-            n_const += 1
-        else:
-            out[fid] = n_var
-            n_var += 1
-    return out
+        row_s, row_c = [], []
+        for v in [R[r][c] for r in range(3) for c in range(3)] + list(t):
+            if isinstance(v, float):
+                row_s.append(-1)
+                row_c.append(v)
+            else:
+                row_s.append(n)
+                row_c.append(0.0)
+                n += 1
+        fslots.append(row_s)
+        fconsts.append(row_c)
+    env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
+    coarse = sorted({env_ix[l] for e in model["self_checks"] for l in e["links"]})
+    checks, _ = danger_boxes(model, cull)
+    joints = sorted({j for (j0, j1, b0), _ in checks if b0 >= 0 for j in (j0, j1)}) or [0]
+    return {"frames": frames, "slots": fslots, "consts": fconsts, "n_frame": n,
+            "coarse": coarse, "coarse_pos": {k: i for i, k in enumerate(coarse)},
+            "joints": joints, "joint_pos": {j: i for i, j in enumerate(joints)},
+            "coarse0": n, "q0": n + 3 * len(coarse), "total": n + 3 * len(coarse) + len(joints)}
 
 
 def _pairs_ab(e):
@@ -565,17 +578,14 @@ def gen_cuda(model: dict) -> str:
         w(stg_if)
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         if True:
-            em1 = Emitter("cuda", SNAP32)
-            fr1 = emit_frames(kin, em1, "q", sc_fn=lambda x, s_, c: "")
-            fv1 = frame_values(kin, fr1)
-            cfs = sorted(((-1 - k, fid) for fid, k in staged_frames(model, kin).items() if k < 0))
-            cf1 = ", ".join("{" + ", ".join(lit32(v) for v in fv1[fidx[fid]]) + "}" for _, fid in cfs) or "{0}"
-            w(f"    // frames of the fine checks whose twelve values are constants (stage index -1 - k)")
-            w(f"    __constant__ float {pre}ConstFrame[{max(1, len(cfs))}][12] = {{{cf1}}};")
-            sid1 = staged_frames(model, kin)
+            lay = stage_layout(model, kin, load_cull(name))
+            nfr = len(lay["slots"])
+            w(f"    // per staged frame and entry: its stage slot, or -1 and the constant value")
+            w(f"    __constant__ int {pre}FrameSlot[{nfr}][12] = {{{', '.join('{' + ', '.join(map(str, r)) + '}' for r in lay['slots'])}}};")
+            w(f"    __constant__ float {pre}FrameConst[{nfr}][12] = {{{', '.join('{' + ', '.join(lit32(v) for v in r) + '}' for r in lay['consts'])}}};")
             env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
             rows_a, rows_b = [], []
-            lvs, fls, lv_n, fl_n = 0, 0, 0, 0
+            lvs, fls = 0, 0
             cull1 = load_cull(name)
             for ci, e in enumerate(model["self_checks"]):
                 A, B = _pairs_ab(e)
@@ -583,22 +593,24 @@ def gen_cuda(model: dict) -> str:
                 fb = kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0]
                 sel = range(len(e["fine"])) if cull1 is None or cull1["live"][ci] is None else cull1["live"][ci]
                 nl, nf = len(list(sel)), len(e["fine"])
-                rows_a.append((env_ix[e["links"][0]], env_ix[e["links"][1]], sid1[fa], sid1[fb]))
+                rows_a.append((lay["coarse_pos"][env_ix[e["links"][0]]], lay["coarse_pos"][env_ix[e["links"][1]]],
+                               lay["frames"][fa], lay["frames"][fb]))
                 rows_b.append((lvs, lvs + nl, fls, fls + nf))
                 lvs += nl
                 fls += nf
-            w(f"    // self-check loop: coarse sphere (env check index) of link A and B, their stage frames;")
+            w(f"    // self-check loop: staged coarse centre of link A and B, their staged frames;")
             w(f"    // live pair range, full pair range")
             w(f"    __constant__ int4 {pre}SelfA[{len(rows_a)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_a)}}};")
             w(f"    __constant__ int4 {pre}SelfB[{len(rows_b)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_b)}}};")
-            w(f"    __constant__ float {pre}CoarseR[{len(model['env_checks'])}] = {{{', '.join(lit32(model['coarse_spheres'][e['link']]['r']) for e in model['env_checks'])}}};")
+            w(f"    __constant__ float {pre}CoarseR[{len(lay['coarse'])}] = {{{', '.join(lit32(model['coarse_spheres'][model['env_checks'][k]['link']]['r']) for k in lay['coarse'])}}};")
             cb_checks, cb_pairs = danger_boxes(model, cull1)
             box = lambda b: "{%s}" % ", ".join(lit32(v) for v in b)  # noqa: E731
             w(f"    // danger boxes (joint space, inside the widened limits): a live pair can come within the")
             w(f"    // culling margin only for joint values inside its box; per self check the two joints and")
             w(f"    // the union of its pairs' boxes (and where its live pairs' boxes start, -1: none), per")
             w(f"    // live pair of an analysed check its box (lo0, hi0, lo1, hi1)")
-            w(f"    __constant__ int4 {pre}SelfJoint[{len(cb_checks)}] = {{{', '.join('{%d, %d, %d, 0}' % c[0] for c in cb_checks)}}};")
+            jp = lay["joint_pos"]
+            w(f"    __constant__ int4 {pre}SelfJoint[{len(cb_checks)}] = {{{', '.join('{%d, %d, %d, 0}' % ((jp[c[0][0]], jp[c[0][1]], c[0][2]) if c[0][2] >= 0 else (0, 0, -1)) for c in cb_checks)}}};")
             w(f"    __constant__ float4 {pre}SelfBox[{len(cb_checks)}] = {{{', '.join(box(c[1]) for c in cb_checks)}}};")
             w(f"    __constant__ float4 {pre}LiveBox[{max(1, len(cb_pairs))}] = {{{', '.join(box(p_) for p_ in cb_pairs) or box((0, 0, 0, 0))}}};")
         w("#endif")
@@ -611,16 +623,15 @@ def gen_cuda(model: dict) -> str:
     w("    static constexpr int kFine = %d;" % len(model["fine_spheres"]))
     w("    static constexpr int kSlots = %d;" % len(slots))
     w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
-    staged_ids = staged_frames(model, kin)
-    w("    // floats of shared-memory staging per thread (frames of the fine checks)")
+    lay = stage_layout(model, kin, load_cull(name))
+    w("    // floats of shared-memory staging per thread (non-constant entries of the fine checks' frames)")
     w("#if defined(VG_FORM_COMPACT)%s" % (" || !defined(VG_STAGED_ALL)" if tabled else ""))
     w("    static constexpr int kStage = 0;")
-    n_stage_frames = sum(1 for v in staged_ids.values() if v >= 0)
     w("#elif defined(VG_SELF_UNROLLED)")
-    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames))
+    w("    static constexpr int kStage = %d;" % lay["n_frame"])
     w("#else")
-    w("    // the coarse link spheres' centres (xyz) and the joint values, read by the self-check loop")
-    w("    static constexpr int kStage = %d;" % (12 * n_stage_frames + 3 * len(model["env_checks"]) + dim))
+    w("    // the coarse centres the self-check loop reads and the joint values its danger boxes test")
+    w("    static constexpr int kStage = %d;" % lay["total"])
     w("#endif")
     w("    static constexpr int kResolution = %d;" % model["resolution"])
     w("    static constexpr float kMinRadius = %s;" % lit32(model["min_radius"]))
@@ -761,7 +772,7 @@ def gen_cuda(model: dict) -> str:
     head = list(em.lines)
     head += limits_code(model, cull)
     fvals = frame_values(kin, fr)
-    sid = staged_frames(model, kin)
+    sid = lay["frames"]
 
     def frame_expr(fid):
         return "vg::Frame{{" + ", ".join(em.ref(v) for v in fvals[fidx[fid]]) + "}}"
@@ -793,11 +804,10 @@ def gen_cuda(model: dict) -> str:
 
     stage = []
     for fid, k in sid.items():
-        if k < 0:
-            continue
         vals = fvals[fidx[fid]]
-        stage.append(" ".join(f"st[{12 * k + j} * vg::kStageStride] = {em.ref(v)};" for j, v in enumerate(vals)) + f"  // {fid}")
-    const_frames = sorted(((-1 - k, fid) for fid, k in sid.items() if k < 0))
+        ws = [f"st[{sl} * vg::kStageStride] = {em.ref(v)};" for sl, v in zip(lay["slots"][k], vals) if sl >= 0]
+        if ws:
+            stage.append(" ".join(ws) + f"  // {fid}")
 
     def env_section(staged):
         out = []
@@ -855,11 +865,11 @@ def gen_cuda(model: dict) -> str:
         return out
 
     compact_body = head + coarse + env_section(False) + self_section(False)
-    c0 = 12 * sum(1 for v in sid.values() if v >= 0)
-    coarse_stage = [" ".join(f"st[{c0 + 3 * k + j} * vg::kStageStride] = cs[{k}].{'xyz'[j]};" for j in range(3))
-                    for k in range(n_env)]
-    qb = c0 + 3 * n_env
-    q_stage = [" ".join(f"st[{qb + d} * vg::kStageStride] = q[{d}];" for d in range(dim))]
+    c0 = lay["coarse0"]
+    coarse_stage = [" ".join(f"st[{c0 + 3 * i + j} * vg::kStageStride] = cs[{k}].{'xyz'[j]};" for j in range(3))
+                    for i, k in enumerate(lay["coarse"])]
+    qb = lay["q0"]
+    q_stage = [" ".join(f"st[{qb + i} * vg::kStageStride] = q[{d}];" for i, d in enumerate(lay["joints"]))]
     self_loop = f"""#pragma unroll 1
 for (int c = 0; c < {len(model['self_checks'])}; ++c)
 {{
@@ -949,25 +959,15 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
         w("        " + l)
     w("    }")
     w("#else")
-    w(f"""    // Frame f of this thread's stage (f >= 0), or constant frame -1 - f.
+    w(f"""    // Staged frame f: its non-constant entries from this thread's stage, the rest constants.
     static __device__ __forceinline__ vg::Frame frame_at(const float *st, int f)
     {{
         vg::Frame r;
-        if (f >= 0)
-        {{
 #pragma unroll
-            for (int c = 0; c < 12; ++c)
-            {{
-                r.m[c] = st[(12 * f + c) * vg::kStageStride];
-            }}
-        }}
-        else
+        for (int c = 0; c < 12; ++c)
         {{
-#pragma unroll
-            for (int c = 0; c < 12; ++c)
-            {{
-                r.m[c] = {pre}ConstFrame[-1 - f][c];
-            }}
+            const int slot = {pre}FrameSlot[f][c];
+            r.m[c] = slot >= 0 ? st[slot * vg::kStageStride] : {pre}FrameConst[f][c];
         }}
         return r;
     }}
