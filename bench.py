@@ -321,7 +321,7 @@ def run_mixed(args, world, rank, local):
         check(lib.vg_autotune_motions(r.encode(), env.handle, a.data_ptr(), b.data_ptr(), 4096, rb.resolution(),
                                       ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), s))
         parts.append({"robot": r, "rb": rb, "env": env, "a": a, "b": b, "out": out,
-                      "pick": {"schedule": "warp per edge" if sched.value == 1 else "segment per edge",
+                      "pick": {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][sched.value],
                                "blocks_per_sm": bps.value or "max", "sample_ms": ms.value}})
 
     def timed(batch):

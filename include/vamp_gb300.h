@@ -84,7 +84,8 @@ int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, floa
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
 /* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):
  * 1 (default) = a warp checks consecutive blocks of one edge, 0 = each lane-block checks its own
- * edge.  No reference counterpart: the reference validates one edge at a time on one core. */
+ * edge, 2 = as 1 with the kernel built for fewer resident blocks and more registers per thread.
+ * No reference counterpart: the reference validates one edge at a time on one core. */
 int vg_env_set_schedule(vg_env *env, int schedule);
 /* Number of objects of a kind (0 spheres, 1 capsules, 2 z-capsules, 3 cuboids, 4 z-cuboids)
  * and the fields of one, in checking order, followed by its min_distance. */
@@ -236,8 +237,9 @@ int vg_validate_motions_learned_device(
  *
  * vg_autotune_motions times the edge-check schedules on the given edges (device buffers, a
  * sample of the caller's workload) and keeps the fastest for this robot in env, where later edge
- * checks of that robot use it: a segment or a warp per edge (*schedule_out 0 / 1) and the
- * resident blocks per SM (*blocks_per_sm_out, 0 = as many as fit); *ms_out is its time on the
+ * checks of that robot use it: a segment per edge (*schedule_out 0), a warp per edge (1), or a
+ * warp per edge built for fewer resident blocks and more registers (2); and the resident
+ * blocks per SM (*blocks_per_sm_out, 0 = as many as fit); *ms_out is its time on the
  * sample.  Verdicts do not depend on the pick.  vg_env_set_schedule clears the picks.
  * Synchronous. */
 int vg_autotune_motions(const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution,

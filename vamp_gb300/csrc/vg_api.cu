@@ -340,8 +340,10 @@ namespace vg
         const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
         const int which = env->lanes == 8 ? 0 : 1;
         const bool learned = m.scores != nullptr;
-        const bool grouped = learned || m.schedule == 1;
-        const void *fn = learned ? r->edges_learned_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]);
+        const bool grouped = learned || m.schedule >= 1;
+        const bool wide = !learned && m.schedule == 2;
+        const void *fn = learned ? r->edges_learned_fn[which]
+                                 : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
         int occ = 0;
         if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
             return rc;
@@ -354,7 +356,8 @@ namespace vg
         const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
         const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
         EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes};
-        const auto launch = learned ? r->edges_learned[which] : (grouped ? r->edges_grouped[which] : r->edges[which]);
+        const auto launch = learned ? r->edges_learned[which]
+                                    : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
         VG_CUDA(launch(p, grid, kBlock, smem, s), "edges kernel launch");
         return VG_OK;
     }
@@ -569,8 +572,8 @@ int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode)
 
 int vg_env_set_schedule(vg_env *env, int schedule)
 {
-    if (!env || (schedule != 0 && schedule != 1))
-        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0 or 1");
+    if (!env || schedule < 0 || schedule > 2)
+        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0, 1 or 2");
     env->schedule = schedule;
     env->tuned.clear();
     return VG_OK;

@@ -236,10 +236,11 @@ int vg_autotune_motions(const char *robot, vg_env *env, const float *a, const fl
     float best = 1e30f;
     const int which = env->lanes == 8 ? 0 : 1;
     const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    for (int sched = 0; sched < 2 && rc == VG_OK; ++sched)
+    for (int sched = 0; sched < 3 && rc == VG_OK; ++sched)
     {
         int occ = 0;
-        rc = prepare_kernel(sched ? r->edges_grouped_fn[which] : r->edges_fn[which], smem, kBlock, &occ);
+        const void *fn = sched == 0 ? r->edges_fn[which] : (sched == 1 ? r->edges_grouped_fn[which] : r->edges_wide_fn[which]);
+        rc = prepare_kernel(fn, smem, kBlock, &occ);
         for (int bps = occ; bps >= 1 && rc == VG_OK; --bps)
         {
             MotionLaunch m{r, env, a, b, n, resolution, nullptr, 0, out, nullptr, env->d_counter, sched, bps};

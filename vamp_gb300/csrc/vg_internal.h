@@ -28,6 +28,9 @@ namespace vg
         // same-edge schedule (a warp checks consecutive blocks of one edge)
         cudaError_t (*edges_grouped[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_grouped_fn[2];
+        // same-edge schedule compiled for fewer resident blocks (more registers per thread)
+        cudaError_t (*edges_wide[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_wide_fn[2];
         // same-edge schedule in a learned block order (EdgesParams::scores)
         cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_learned_fn[2];
@@ -61,7 +64,7 @@ namespace vg
     struct RobotTune
     {
         const RobotOps *robot;
-        int schedule;       // 0: a segment per edge, 1: a warp per edge
+        int schedule;       // 0: a segment per edge, 1: a warp per edge, 2: a warp per edge, register-rich build
         int blocks_per_sm;  // resident blocks per SM (0: as many as fit)
     };
 }  // namespace vg
@@ -112,7 +115,7 @@ namespace vg
         uint8_t *out;
         int32_t *blocks;
         unsigned *counter;     // work counter, cleared on the stream before the launch
-        int schedule = 1;      // 0: a segment per edge, 1: a warp per edge
+        int schedule = 1;      // 0: a segment per edge, 1: a warp per edge, 2: the same, register-rich build
         int blocks_per_sm = 0;  // 0: as many as fit
     };
 

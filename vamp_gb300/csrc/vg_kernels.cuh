@@ -16,7 +16,12 @@
 
 // Resident blocks of 128 threads per SM the kernels are compiled for (caps their registers).
 #ifndef VG_MIN_BLOCKS
-#define VG_MIN_BLOCKS 3
+#define VG_MIN_BLOCKS 4
+#endif
+// The register-rich variant of the same-edge kernel (fewer resident blocks, no register cap
+// below 168): the autotuner picks it where it is faster (pointcloud scenes).
+#ifndef VG_MIN_BLOCKS_WIDE
+#define VG_MIN_BLOCKS_WIDE 3
 #endif
 
 namespace vg
@@ -336,8 +341,8 @@ namespace vg
     // (block i = block 0 minus v / (W n), i times).  The edge is invalid if any checked block is,
     // and the reference would have stopped at the first invalid block, so the block count
     // reported is that block's index + 1.
-    template <typename Robot, int W, bool kLearned>
-    __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_grouped_kernel(EdgesParams p)
+    template <typename Robot, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS>
+    __global__ void __launch_bounds__(128, kMinBlocks) edges_grouped_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
         const EnvView ev = stage_env(p.env, smem);
