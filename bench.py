@@ -224,6 +224,19 @@ def cpu_baseline(scene, a, b, budget_s: float = 10.0):
             "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
 
 
+def autotune(robot: str, env, a, b, resolution: int, stream, sample: int = 4096) -> dict:
+    """Runs the library's autotuner on the first `sample` edges; returns its pick."""
+    import ctypes
+
+    from vamp_gb300._lib import check, lib
+
+    sched, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    check(lib.vg_autotune_motions(robot.encode(), env.handle, a.data_ptr(), b.data_ptr(), min(sample, len(a)), resolution,
+                                  ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), stream))
+    return {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][sched.value],
+            "blocks_per_sm": bps.value or "max", "sample_edges": min(sample, len(a)), "sample_ms": ms.value}
+
+
 def run_capt(args, world, rank, local):
     """Pointcloud workload: Panda with 50,000 points sampled on the surfaces of 30 random cuboids
     and cylinders plus 2% uniform noise, checked through the CAPT built with the Panda's radius
@@ -250,6 +263,7 @@ def run_capt(args, world, rank, local):
     qo = torch.empty(len(q), dtype=torch.uint8, device=dev)
     eo = torch.empty(len(a), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
+    pick = autotune("panda", env, a, b, RESOLUTION, stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def states():
@@ -279,7 +293,7 @@ def run_capt(args, world, rank, local):
             "states_per_s": (1 << 20) / (res["states"] / 1e3), "states_ms": res["states"],
             "edges_per_s": 16384 / (res["edges"] / 1e3), "edges_ms": res["edges"],
             "capt_build_s": build_s, "capt_blocks": int(env.pointcloud_layout(0)["aff_starts"][-1]),
-            "valid_states": float(qo.float().mean()), "valid_edges": float(eo.float().mean()),
+            "valid_states": float(qo.float().mean()), "valid_edges": float(eo.float().mean()), "autotuner": pick,
             "steps": args.steps, "warmup": args.warmup}))
 
 
@@ -317,12 +331,8 @@ def run_mixed(args, world, rank, local):
         a_np, b_np = scenes.edges(rb.s_m, rb.s_a, MIXED_EDGES, EDGE_SEED + 1 + i)
         a, b = torch.from_numpy(a_np).to(dev), torch.from_numpy(b_np).to(dev)
         out = torch.empty(MIXED_EDGES, dtype=torch.uint8, device=dev)
-        sched, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
-        check(lib.vg_autotune_motions(r.encode(), env.handle, a.data_ptr(), b.data_ptr(), 4096, rb.resolution(),
-                                      ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), s))
         parts.append({"robot": r, "rb": rb, "env": env, "a": a, "b": b, "out": out,
-                      "pick": {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][sched.value],
-                               "blocks_per_sm": bps.value or "max", "sample_ms": ms.value}})
+                      "pick": autotune(r, env, a, b, rb.resolution(), s)})
 
     def timed(batch):
         for _ in range(max(args.warmup, 3)):
@@ -535,11 +545,15 @@ def run_gpu(args, world, rank, local):
     dev = torch.device("cuda", local)
     scene, a_np, b_np = workload()
     env = vg.Environment.from_scene(scene)
-    env.set_schedule(args.schedule)
     a = torch.from_numpy(a_np).to(dev)
     b = torch.from_numpy(b_np).to(dev)
     out = torch.empty(N_EDGES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
+    if args.schedule is None:
+        pick = autotune("panda", env, a, b, RESOLUTION, stream.cuda_stream)
+    else:
+        env.set_schedule(args.schedule)
+        pick = {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][args.schedule]}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def launch():
@@ -603,7 +617,7 @@ def run_gpu(args, world, rank, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded scene and edges)",
-        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "order": "plain (reference block order)", "schedule": "warp per edge" if args.schedule == 1 else "lane-block per edge",
+        "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "order": "plain (reference block order)", "autotuner": pick,
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
                    "colliding_fraction": float(1 - gpu_verdicts.mean())},
         "gpu_launches": args.steps,
@@ -635,7 +649,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-order measurement")
     ap.add_argument("--labels", type=int, default=2 << 20, help="exact-checker labels the learned order trains on")
-    ap.add_argument("--schedule", type=int, default=1, help="GPU edge schedule: 1 warp per edge, 0 lane-block per edge")
+    ap.add_argument("--schedule", type=int, default=None,
+                    help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
+                         "2 warp per edge with the register-rich build")
     ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
                          "mixed: four robots in one CUDA graph")
