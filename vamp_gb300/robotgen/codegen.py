@@ -382,7 +382,7 @@ TABLED = {"ur5", "fetch", "baxter"}
 # 1.570796325 leave ~1e-9 residues that only cost operations (their effect is below 1e-8 m)
 SNAP32 = 1e-7
 # coarse environment queries evaluated together in one pass over the objects
-COARSE_BATCH = int(os.environ.get("VG_COARSE_BATCH", "6"))
+COARSE_BATCH = int(os.environ.get("VG_COARSE_BATCH", "4"))
 
 
 def f32_down(v: float) -> float:
