@@ -172,6 +172,17 @@ def algorithmic_flops(scene, a, b, sample: int = 8192):
             "tests": sum(int(t) for t in cnt.tests) * scale, "per_lane_fk": per_lane_fk}
 
 
+def profiled_traffic():
+    """DRAM bytes (read + write) per launch of the edge kernel, from the committed ncu summary."""
+    import re
+
+    try:
+        text = (ROOT / "profiles" / "edges_grouped_panda_65536.md").read_text()
+        return int(re.search(r"traffic_bytes_per_launch: (\d+)", text).group(1))
+    except Exception:
+        return None
+
+
 def fp32_peak_tflops(device_props, sm_mhz: float | None):
     """FP32 (non-tensor) peak: 128 FP32 lanes x 2 FLOP per SM per clock."""
     sms = device_props.multi_processor_count
@@ -630,7 +641,7 @@ def run_gpu(args, world, rank, local):
     peak, mhz, sms = fp32_peak_tflops(torch.cuda.get_device_properties(dev), clk["sm_mhz"] if clk else None)
     achieved = work["flops"] / (kernel_ms / 1e3) / 1e12
     line["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                        "traffic": None,
+                        "traffic": profiled_traffic(),
                         "note": f"FP32 peak = {sms} SMs x 256 FLOP/clk x {mhz:.0f} MHz (max SM clock of MEASURED_PEAKS.json); "
                                 f"algorithmic FLOPs counted by the CPU oracle on 8192 of the edges, scaled"}
     if not args.no_cpu:
