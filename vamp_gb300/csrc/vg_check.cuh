@@ -604,6 +604,8 @@ namespace vg
     // Threads per block of every checking kernel, and the stride of the per-thread columns of
     // the robots' shared-memory stage.
     constexpr int kStageStride = 128;
+    // words of per-warp shared scratch available to a generated fkcc (environment checks per robot)
+    constexpr int kWarpScratch = 64;
 
     // The context a generated Robot::fkcc body runs against.
     template <int W>
@@ -617,6 +619,8 @@ namespace vg
         bool in_limits = false;
         // this thread's column of the robot's shared-memory stage: element i at stage[i * kStageStride]
         float *stage = nullptr;
+        // this warp's scratch (kWarpScratch words) for warp-uniform values such as per-link hit masks
+        unsigned *wsc = nullptr;
 
         __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
         {

@@ -73,7 +73,9 @@ namespace vg
     template <typename Robot, int W>
     __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
-        CheckCtx<W> ctx{ev, alive, false, stage};
+        static_assert(Robot::kEnvChecks <= kWarpScratch, "per-warp scratch holds one word per environment check");
+        __shared__ unsigned warp_scratch[kStageStride / 32][kWarpScratch];
+        CheckCtx<W> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
         Robot::fkcc(q, ctx);
         return ctx.alive;
     }

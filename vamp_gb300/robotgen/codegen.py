@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import math
 import os
 from pathlib import Path
@@ -448,13 +449,33 @@ def limits_code(model: dict, cull) -> list:
     return lines
 
 
+def _aliases(lines) -> dict:
+    """name -> (name, sign) for the emitted copies `const float A = B;` and `const float A = (-B);`."""
+    out = {}
+    for line in lines:
+        m = re.fullmatch(r"const float (\w+) = (?:\(-(\w+)\)|(\w+));", line.strip())
+        if m:
+            out[m.group(1)] = (m.group(2), -1) if m.group(2) else (m.group(3), 1)
+    return out
+
+
 def stage_layout(model: dict, kin, cull) -> dict:
-    """The staged form's shared-memory stage, per thread: the non-constant entries of the frames
-    the fine checks use (in first-use order), then the centres of the coarse spheres the self
-    loop reads, then the joint values the danger boxes test."""
+    """The staged form's shared-memory stage, per thread: each distinct non-constant value among
+    the entries of the frames the fine checks use (an entry that is a copy or the negation of
+    another takes that value's slot and a sign), then the centres of every coarse sphere, then
+    the joint values the danger boxes test."""
     slots, _ = slot_table(model)
     em = Emitter("cuda", SNAP32)
     fr = emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
+    alias = _aliases(em.lines)
+
+    def resolve(name):
+        sign = 1
+        while name in alias:
+            name, sg = alias[name]
+            sign *= sg
+        return name, sign
+
     order = []
     for e in model["env_checks"]:
         order.append(kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0])
@@ -462,7 +483,7 @@ def stage_layout(model: dict, kin, cull) -> dict:
         A, B = _pairs_ab(e)
         order.append(kin.sphere_in_frame(slots[A[0]][0], slots[A[0]][1])[0])
         order.append(kin.sphere_in_frame(slots[B[0]][0], slots[B[0]][1])[0])
-    frames, fslots, fconsts, n = {}, [], [], 0
+    frames, fslots, fconsts, values = {}, [], [], {}
     for fid in order:
         if fid in frames:
             continue
@@ -473,20 +494,24 @@ def stage_layout(model: dict, kin, cull) -> dict:
             if isinstance(v, float):
                 row_s.append(-1)
                 row_c.append(v)
-            else:
-                row_s.append(n)
-                row_c.append(0.0)
-                n += 1
+                continue
+            neg = v.startswith("-")
+            base, sign = resolve(v[1:] if neg else v)
+            sign = -sign if neg else sign
+            if base not in values:
+                values[base] = len(values)
+            row_s.append(values[base] if sign > 0 else -2 - values[base])
+            row_c.append(0.0)
         fslots.append(row_s)
         fconsts.append(row_c)
-    env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
-    coarse = sorted({env_ix[l] for e in model["self_checks"] for l in e["links"]})
+    n = len(values)
+    n_env = len(model["env_checks"])
     checks, _ = danger_boxes(model, cull)
     joints = sorted({j for (j0, j1, b0), _ in checks if b0 >= 0 for j in (j0, j1)}) or [0]
-    return {"frames": frames, "slots": fslots, "consts": fconsts, "n_frame": n,
-            "coarse": coarse, "coarse_pos": {k: i for i, k in enumerate(coarse)},
+    return {"frames": frames, "slots": fslots, "consts": fconsts, "n_frame": n, "values": list(values),
+            "coarse": list(range(n_env)), "coarse_pos": {k: k for k in range(n_env)},
             "joints": joints, "joint_pos": {j: i for i, j in enumerate(joints)},
-            "coarse0": n, "q0": n + 3 * len(coarse), "total": n + 3 * len(coarse) + len(joints)}
+            "coarse0": n, "q0": n + 3 * n_env, "total": n + 3 * n_env + len(joints)}
 
 
 def _pairs_ab(e):
@@ -554,9 +579,9 @@ def gen_cuda(model: dict) -> str:
         # tables of the table-driven form: only where that form is compiled
         tab_if = "#ifndef VG_STAGED_ALL" if tabled else "#if 0"
         stg_if = "#ifdef VG_STAGED_ALL" if tabled else "#if 1"
+        w(f"    __constant__ int {pre}EnvStart[{len(env_start)}] = {{{', '.join(map(str, env_start))}}};")
         w(tab_if)
         w(f"    __constant__ int {pre}EnvCoarse[{len(model['env_checks'])}] = {{{', '.join(str(coarse_slot[e['link']]) for e in model['env_checks'])}}};")
-        w(f"    __constant__ int {pre}EnvStart[{len(env_start)}] = {{{', '.join(map(str, env_start))}}};")
         w("#endif")
         w(f"    __constant__ int {pre}EnvFine[{len(env_fine)}] = {{{', '.join(map(str, env_fine))}}};")
         w(tab_if)
@@ -580,7 +605,12 @@ def gen_cuda(model: dict) -> str:
         if True:
             lay = stage_layout(model, kin, load_cull(name))
             nfr = len(lay["slots"])
-            w(f"    // per staged frame and entry: its stage slot, or -1 and the constant value")
+            env_frames = [lay["frames"][kin.sphere_in_frame(slots[e["fine"][0]][0], slots[e["fine"][0]][1])[0]]
+                          for e in model["env_checks"]]
+            w(f"    // staged frame of each environment check's fine spheres")
+            w(f"    __constant__ int {pre}EnvFrameS[{len(env_frames)}] = {{{', '.join(map(str, env_frames))}}};")
+            w(f"    // per staged frame and entry: its stage slot s (value st[s]), -2 - s (value -st[s]), or -1")
+            w(f"    // and the constant value")
             w(f"    __constant__ int {pre}FrameSlot[{nfr}][12] = {{{', '.join('{' + ', '.join(map(str, r)) + '}' for r in lay['slots'])}}};")
             w(f"    __constant__ float {pre}FrameConst[{nfr}][12] = {{{', '.join('{' + ', '.join(lit32(v) for v in r) + '}' for r in lay['consts'])}}};")
             env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
@@ -623,6 +653,7 @@ def gen_cuda(model: dict) -> str:
     w("    static constexpr int kFine = %d;" % len(model["fine_spheres"]))
     w("    static constexpr int kSlots = %d;" % len(slots))
     w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
+    w("    static constexpr int kEnvChecks = %d;" % len(model["env_checks"]))
     lay = stage_layout(model, kin, load_cull(name))
     w("    // floats of shared-memory staging per thread (non-constant entries of the fine checks' frames)")
     w("#if defined(VG_FORM_COMPACT)%s" % (" || !defined(VG_STAGED_ALL)" if tabled else ""))
@@ -803,11 +834,9 @@ def gen_cuda(model: dict) -> str:
         base += size
 
     stage = []
-    for fid, k in sid.items():
-        vals = fvals[fidx[fid]]
-        ws = [f"st[{sl} * vg::kStageStride] = {em.ref(v)};" for sl, v in zip(lay["slots"][k], vals) if sl >= 0]
-        if ws:
-            stage.append(" ".join(ws) + f"  // {fid}")
+    vals_ = lay["values"]
+    for i in range(0, len(vals_), 6):
+        stage.append(" ".join(f"st[{j} * vg::kStageStride] = {vals_[j]};" for j in range(i, min(i + 6, len(vals_)))))
 
     def env_section(staged):
         out = []
@@ -903,7 +932,47 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
     }}
 }}""".split("\n")
     staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
-    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse + coarse_stage + env_section(True)
+    cut = next(i for i, l in enumerate(coarse) if l.startswith("unsigned ch["))
+    nb = -(-n_env // 4)
+    env_loops = f"""// coarse spheres of every environment-checked link, 4 at a time (one copy of the batched query)
+unsigned *const chs = ctx.wsc;
+#pragma unroll 1
+for (int b = 0; b < {nb}; ++b)
+{{
+    float4 sp[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {{
+        const int k = 4 * b + s;
+        // padding sphere: far away with radius -inf, it is never tested and never hits
+        sp[s] = k < {n_env} ? make_float4(st[({c0} + 3 * k) * vg::kStageStride], st[({c0} + 3 * k + 1) * vg::kStageStride],
+                                          st[({c0} + 3 * k + 2) * vg::kStageStride], {pre}CoarseR[k])
+                            : make_float4(1.0e10f, 0.0f, 0.0f, -__int_as_float(0x7f800000));
+    }}
+    unsigned h[4];
+    ctx.template env_many<4>(sp, ctx.alive, h);
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {{
+        if (4 * b + s < {n_env} && (threadIdx.x & 31) == 0)
+        {{
+            chs[4 * b + s] = h[s];  // warp-uniform
+        }}
+    }}
+}}
+__syncwarp();
+// fine spheres of the links whose coarse sphere hit
+#pragma unroll 1
+for (int k = 0; k < {n_env}; ++k)
+{{
+    const unsigned need = chs[k] & ctx.alive;
+    if (need)
+    {{
+        const unsigned hit = env_fine<Ctx::kW>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
+        if (hit && !(ctx.alive &= ~hit)) return;
+    }}
+}}""".split("\n")
+    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut] + coarse_stage + env_loops
                    + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
@@ -967,7 +1036,9 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
         for (int c = 0; c < 12; ++c)
         {{
             const int slot = {pre}FrameSlot[f][c];
-            r.m[c] = slot >= 0 ? st[slot * vg::kStageStride] : {pre}FrameConst[f][c];
+            const int at = slot >= 0 ? slot : -2 - slot;
+            const float v = slot == -1 ? {pre}FrameConst[f][c] : st[at * vg::kStageStride];
+            r.m[c] = slot < -1 ? -v : v;
         }}
         return r;
     }}
