@@ -972,7 +972,13 @@ for (int k = 0; k < {n_env}; ++k)
         if (hit && !(ctx.alive &= ~hit)) return;
     }}
 }}""".split("\n")
-    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut] + coarse_stage + env_loops
+    # variant: the coarse queries unrolled on the centres in registers, the fine section looped
+    k_fine = next(i for i, l in enumerate(env_loops) if l.startswith("// fine spheres of the links"))
+    coarse_unrolled = (coarse[cut:] + ["unsigned *const chs = ctx.wsc;", "if ((threadIdx.x & 31) == 0)", "{"]
+                       + [f"    chs[{k}] = ch[{k}];" for k in range(n_env)] + ["}", "__syncwarp();"])
+    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut] + coarse_stage
+                   + ["#ifdef VG_COARSE_UNROLLED"] + coarse_unrolled + env_loops[k_fine:]
+                   + ["#else"] + env_loops + ["#endif"]
                    + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
