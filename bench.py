@@ -235,8 +235,9 @@ def cpu_baseline(scene, a, b, budget_s: float = 10.0):
             "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
 
 
-def autotune(robot: str, env, a, b, resolution: int, stream, sample: int = 4096) -> dict:
-    """Runs the library's autotuner on the first `sample` edges; returns its pick."""
+def autotune(robot: str, env, a, b, resolution: int, stream, sample: int = 65536) -> dict:
+    """Runs the library's autotuner on the first `sample` edges (a persistent launch needs a
+    sample of the workload's own size to show its tail); returns its pick."""
     import ctypes
 
     from vamp_gb300._lib import check, lib
