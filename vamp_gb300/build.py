@@ -62,9 +62,6 @@ def _defines() -> list[str]:
         out.append("-DVG_STAGED_ALL")
     # VG_CAPT_SHARED_WEIGHT=w: the pointcloud query scans one lane's list with the whole warp
     # when 4 x the longest list exceeds w x the warp's shared steps
-    # VG_COARSE_UNROLLED=1: staged form with the coarse environment queries unrolled
-    if os.environ.get("VG_COARSE_UNROLLED") == "1":
-        out.append("-DVG_COARSE_UNROLLED")
     w = os.environ.get("VG_CAPT_SHARED_WEIGHT")
     if w:
         out.append(f"-DVG_CAPT_SHARED_WEIGHT={int(w)}")

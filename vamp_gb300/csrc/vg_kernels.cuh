@@ -70,13 +70,14 @@ namespace vg
         return v;
     }
 
-    template <typename Robot, int W>
+    // kLoopedEnv: the robot's environment section as loops (smaller code) instead of unrolled
+    template <typename Robot, int W, bool kLoopedEnv = false>
     __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
         static_assert(Robot::kEnvChecks <= kWarpScratch, "per-warp scratch holds one word per environment check");
         __shared__ unsigned warp_scratch[kStageStride / 32][kWarpScratch];
         CheckCtx<W> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
-        Robot::fkcc(q, ctx);
+        Robot::template fkcc<CheckCtx<W>, kLoopedEnv>(q, ctx);
         return ctx.alive;
     }
 
@@ -111,7 +112,7 @@ namespace vg
             {
                 q[d] = in ? p.q[idx * D + d] : 0.0f;
             }
-            const unsigned alive = run_fkcc<Robot, 1>(ev, q, __ballot_sync(kFull, in), stage);
+            const unsigned alive = run_fkcc<Robot, 1, true>(ev, q, __ballot_sync(kFull, in), stage);
             if (in)
             {
                 p.out[idx] = static_cast<uint8_t>((alive >> (threadIdx.x & 31)) & 1u);
@@ -343,7 +344,7 @@ namespace vg
     // (block i = block 0 minus v / (W n), i times).  The edge is invalid if any checked block is,
     // and the reference would have stopped at the first invalid block, so the block count
     // reported is that block's index + 1.
-    template <typename Robot, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS>
+    template <typename Robot, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = false>
     __global__ void __launch_bounds__(128, kMinBlocks) edges_grouped_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
@@ -432,7 +433,7 @@ namespace vg
                         }
                     }
                     const unsigned mask = __ballot_sync(kFull, active);
-                    const unsigned alive = run_fkcc<Robot, W>(ev, q, mask, stage);
+                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv>(ev, q, mask, stage);
                     const unsigned dead = mask & ~alive;
                     // one bit per active segment (its first lane)
                     const unsigned leaders = mask & kSegLeaders;
@@ -461,7 +462,7 @@ namespace vg
                 {
                     const bool active = i0 + seg < n;
                     const unsigned mask = __ballot_sync(kFull, active);
-                    const unsigned alive = run_fkcc<Robot, W>(ev, q, mask, stage);
+                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv>(ev, q, mask, stage);
                     const unsigned dead = mask & ~alive;
                     if (dead)
                     {

@@ -20,10 +20,10 @@ namespace vg
         return cudaGetLastError();
     }
 
-    template <typename R, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS>
+    template <typename R, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = false>
     cudaError_t launch_edges_grouped(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        edges_grouped_kernel<R, W, kLearned, kMinBlocks><<<grid, block, smem, s>>>(p);
+        edges_grouped_kernel<R, W, kLearned, kMinBlocks, kLoopedEnv><<<grid, block, smem, s>>>(p);
         return cudaGetLastError();
     }
 
@@ -62,10 +62,10 @@ namespace vg
         o.edges_grouped[1] = &launch_edges_grouped<R, 4, false>;
         o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false>);
         o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false>);
-        o.edges_wide[0] = &launch_edges_grouped<R, 8, false, VG_MIN_BLOCKS_WIDE>;
-        o.edges_wide[1] = &launch_edges_grouped<R, 4, false, VG_MIN_BLOCKS_WIDE>;
-        o.edges_wide_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false, VG_MIN_BLOCKS_WIDE>);
-        o.edges_wide_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false, VG_MIN_BLOCKS_WIDE>);
+        o.edges_wide[0] = &launch_edges_grouped<R, 8, false, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_wide[1] = &launch_edges_grouped<R, 4, false, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_wide_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false, VG_MIN_BLOCKS_WIDE, true>);
+        o.edges_wide_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false, VG_MIN_BLOCKS_WIDE, true>);
         o.edges_learned[0] = &launch_edges_grouped<R, 8, true>;
         o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
         o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);

@@ -721,7 +721,7 @@ def gen_cuda(model: dict) -> str:
     }}
 
     // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.
-    template <typename Ctx>
+    template <typename Ctx, bool kLoopedEnv = false>
     static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)
     {{
         float F[kFrames * 12];
@@ -972,13 +972,11 @@ for (int k = 0; k < {n_env}; ++k)
         if (hit && !(ctx.alive &= ~hit)) return;
     }}
 }}""".split("\n")
-    # variant: the coarse queries unrolled on the centres in registers, the fine section looped
-    k_fine = next(i for i, l in enumerate(env_loops) if l.startswith("// fine spheres of the links"))
-    coarse_unrolled = (coarse[cut:] + ["unsigned *const chs = ctx.wsc;", "if ((threadIdx.x & 31) == 0)", "{"]
-                       + [f"    chs[{k}] = ch[{k}];" for k in range(n_env)] + ["}", "__syncwarp();"])
+    # the environment section either as loops (one copy of the batched query: small code) or
+    # unrolled (the coarse centres stay in registers: fewer instructions); chosen per kernel
     looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut] + coarse_stage
-                   + ["#ifdef VG_COARSE_UNROLLED"] + coarse_unrolled + env_loops[k_fine:]
-                   + ["#else"] + env_loops + ["#endif"]
+                   + ["if constexpr (kLoopedEnv)", "{"] + ["    " + l for l in env_loops] + ["}", "else", "{"]
+                   + ["    " + l for l in coarse[cut:] + env_section(True)] + ["}"]
                    + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
@@ -1027,7 +1025,7 @@ for (int k = 0; k < {n_env}; ++k)
     }}
 """)
     w("    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.")
-    w("    template <typename Ctx>")
+    w("    template <typename Ctx, bool kLoopedEnv = false>")
     w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
     w("    {")
     for l in compact_body:
@@ -1130,7 +1128,7 @@ for (int k = 0; k < {n_env}; ++k)
     }}
 """)
     w("    // Robot::fkcc for the lanes of ctx.alive.  Clears the lanes of every segment found in collision.")
-    w("    template <typename Ctx>")
+    w("    template <typename Ctx, bool kLoopedEnv = false>")
     w("    static __device__ __forceinline__ void fkcc(const float *q, Ctx &ctx)")
     w("    {")
     w("#ifdef VG_SELF_UNROLLED")
