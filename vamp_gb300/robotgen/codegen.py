@@ -467,7 +467,8 @@ def stage_layout(model: dict, kin, cull) -> dict:
     slots, _ = slot_table(model)
     em = Emitter("cuda", SNAP32)
     fr = emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
-    alias = _aliases(em.lines)
+    # VG_STAGE_NO_DEDUP=1 (generator switch): one slot per frame entry, copies included
+    alias = {} if os.environ.get("VG_STAGE_NO_DEDUP") == "1" else _aliases(em.lines)
 
     def resolve(name):
         sign = 1
@@ -974,9 +975,9 @@ for (int k = 0; k < {n_env}; ++k)
 }}""".split("\n")
     # the environment section either as loops (one copy of the batched query: small code) or
     # unrolled (the coarse centres stay in registers: fewer instructions); chosen per kernel
-    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut] + coarse_stage
-                   + ["if constexpr (kLoopedEnv)", "{"] + ["    " + l for l in env_loops] + ["}", "else", "{"]
-                   + ["    " + l for l in coarse[cut:] + env_section(True)] + ["}"]
+    looped_body = (head + ["float *const st = ctx.stage;"] + stage + q_stage + coarse[:cut]
+                   + ["if constexpr (kLoopedEnv)", "{"] + ["    " + l for l in coarse_stage + env_loops] + ["}", "else", "{"]
+                   + ["    " + l for l in coarse[cut:] + coarse_stage + env_section(True)] + ["}"]
                    + ["// self-collision link pairs, in the reference's order"] + self_loop)
 
     w("#ifdef VG_FORM_COMPACT")
