@@ -461,9 +461,9 @@ def _aliases(lines) -> dict:
 
 def stage_layout(model: dict, kin, cull) -> dict:
     """The staged form's shared-memory stage, per thread: each distinct non-constant value among
-    the entries of the frames the fine checks use (an entry that is a copy or the negation of
-    another takes that value's slot and a sign), then the centres of every coarse sphere, then
-    the joint values the danger boxes test."""
+    the entries of the frames the fine checks use (an entry that is a copy of another takes that
+    value's slot), then the centres of every coarse sphere, then the joint values the danger
+    boxes test."""
     slots, _ = slot_table(model)
     em = Emitter("cuda", SNAP32)
     fr = emit_frames(kin, em, "q", sc_fn=lambda x, s_, c: "")
@@ -499,9 +499,12 @@ def stage_layout(model: dict, kin, cull) -> dict:
             neg = v.startswith("-")
             base, sign = resolve(v[1:] if neg else v)
             sign = -sign if neg else sign
-            if base not in values:
-                values[base] = len(values)
-            row_s.append(values[base] if sign > 0 else -2 - values[base])
+            # a negated copy gets its own slot: decoding a sign per entry costs more in the fine
+            # checks than the slot saves
+            key = base if sign > 0 else "-" + base
+            if key not in values:
+                values[key] = len(values)
+            row_s.append(values[key])
             row_c.append(0.0)
         fslots.append(row_s)
         fconsts.append(row_c)
@@ -610,8 +613,7 @@ def gen_cuda(model: dict) -> str:
                           for e in model["env_checks"]]
             w(f"    // staged frame of each environment check's fine spheres")
             w(f"    __constant__ int {pre}EnvFrameS[{len(env_frames)}] = {{{', '.join(map(str, env_frames))}}};")
-            w(f"    // per staged frame and entry: its stage slot s (value st[s]), -2 - s (value -st[s]), or -1")
-            w(f"    // and the constant value")
+            w(f"    // per staged frame and entry: its stage slot, or -1 and the constant value")
             w(f"    __constant__ int {pre}FrameSlot[{nfr}][12] = {{{', '.join('{' + ', '.join(map(str, r)) + '}' for r in lay['slots'])}}};")
             w(f"    __constant__ float {pre}FrameConst[{nfr}][12] = {{{', '.join('{' + ', '.join(lit32(v) for v in r) + '}' for r in lay['consts'])}}};")
             env_ix = {e["link"]: k for k, e in enumerate(model["env_checks"])}
@@ -835,7 +837,7 @@ def gen_cuda(model: dict) -> str:
         base += size
 
     stage = []
-    vals_ = lay["values"]
+    vals_ = [f"(-{v[1:]})" if v.startswith("-") else v for v in lay["values"]]
     for i in range(0, len(vals_), 6):
         stage.append(" ".join(f"st[{j} * vg::kStageStride] = {vals_[j]};" for j in range(i, min(i + 6, len(vals_)))))
 
@@ -1041,9 +1043,7 @@ for (int k = 0; k < {n_env}; ++k)
         for (int c = 0; c < 12; ++c)
         {{
             const int slot = {pre}FrameSlot[f][c];
-            const int at = slot >= 0 ? slot : -2 - slot;
-            const float v = slot == -1 ? {pre}FrameConst[f][c] : st[at * vg::kStageStride];
-            r.m[c] = slot < -1 ? -v : v;
+            r.m[c] = slot >= 0 ? st[slot * vg::kStageStride] : {pre}FrameConst[f][c];
         }}
         return r;
     }}
