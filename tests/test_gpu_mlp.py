@@ -179,14 +179,15 @@ def test_learned_order_keeps_every_verdict_and_checks_fewer_blocks(torch, traine
     assert np.all(learned_blocks[coll] >= 1)
 
 
-@pytest.mark.parametrize("kind", ["random", "nan", "inf", "constant"])
-def test_any_scores_keep_every_verdict(torch, kind):
-    """The order is a permutation of each edge's blocks whatever the scores hold."""
+@pytest.mark.parametrize("kind,lanes", [("random", 8), ("nan", 8), ("inf", 8), ("constant", 8), ("random", 4), ("constant", 4)])
+def test_any_scores_keep_every_verdict(torch, kind, lanes):
+    """The order is a permutation of each edge's blocks whatever the scores hold (8-lane blocks
+    with the x86 bound, 4-lane blocks with the exact square root)."""
     from vamp_gb300 import scenes
     import vamp_gb300 as vg
-    from vamp_gb300._lib import lib
+    from vamp_gb300._lib import SQRT_EXACT, SQRT_X86, lib
 
-    env = vg.Environment.from_scene(scenes.scene_config1(2))
+    env = vg.Environment.from_scene(scenes.scene_config1(2), lanes=lanes, sqrt_mode=SQRT_X86 if lanes == 8 else SQRT_EXACT)
     a, b = scenes.edges(vg.panda.s_m, vg.panda.s_a, 8192, 31)
     n, probes = len(a), 32
     rng = np.random.default_rng(7)
