@@ -257,3 +257,134 @@ panda = Robot("panda")
 ur5 = Robot("ur5")
 fetch = Robot("fetch")
 baxter = Robot("baxter")
+
+
+# ------------------------------------------------------------------ autotuning, batches, learning
+# None of these has a counterpart in the reference's bindings; they wrap the C ABI's batch,
+# autotuner and learned-ordering entry points (include/vamp_gb300.h).  Device buffers are torch
+# CUDA tensors; calls run on the current stream.
+
+SCHEDULES = ("segment per edge", "warp per edge", "warp per edge, register-rich build")
+
+
+def _stream(t):
+    import torch
+
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def autotune(robot: Robot, environment: Environment, starts, goals, resolution: int | None = None) -> dict:
+    """Times the edge-check schedules on these edges (CUDA tensors: a sample of the workload,
+    best of the workload's own size) and keeps the fastest for this robot in `environment`."""
+    res = robot.resolution() if resolution is None else int(resolution)
+    a, b = starts.contiguous(), goals.contiguous()
+    sched, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    check(lib.vg_autotune_motions(robot.name.encode(), environment.handle, a.data_ptr(), b.data_ptr(), a.shape[0], res,
+                                  ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), _stream(a)))
+    return {"schedule": SCHEDULES[sched.value], "blocks_per_sm": bps.value or None, "ms": ms.value}
+
+
+class CollisionPredictor:
+    """The learned block ordering's network for one robot: sin/cos features -> 256 -> 256 -> 1,
+    BF16 weights, FP32 accumulation, trained on the GPU (tcgen05 kernels) on exact verdicts."""
+
+    def __init__(self, robot: Robot, seed: int = 0):
+        self.robot = robot
+        self._h = lib.vg_mlp_create(robot.dimension(), seed)
+        if not self._h:
+            check(-1)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.vg_mlp_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def train(self, configurations, valid, epochs: int = 3, batch: int = 1024, lr: float = 1e-3) -> np.ndarray:
+        """Adam on (configurations [n][dim] float32, valid [n] uint8: 1 = collision free) CUDA
+        tensors; returns the mean loss of each epoch."""
+        q, v = configurations.contiguous(), valid.contiguous()
+        losses = np.zeros(epochs, np.float32)
+        check(lib.vg_mlp_train_device(self._h, q.data_ptr(), v.data_ptr(), q.shape[0], epochs, batch, float(lr),
+                                      _ptr(losses), _stream(q)))
+        return losses
+
+    def train_on_environment(self, environment: Environment, n: int = 1 << 21, epochs: int = 3, seed: int = 1):
+        """Labels n uniform configurations with the exact checker in `environment`, then trains."""
+        import torch
+
+        from . import scenes
+
+        q = torch.from_numpy(scenes.configurations(self.robot.s_m, self.robot.s_a, n, seed)).cuda()
+        valid = self.robot.validate_batch(q, environment)
+        return self.train(q, valid, epochs)
+
+    def predict(self, configurations):
+        """Collision probability per configuration (CUDA tensor in and out; fused inference)."""
+        import torch
+
+        q = configurations.contiguous()
+        p = torch.empty(q.shape[0], dtype=torch.float32, device=q.device)
+        check(lib.vg_mlp_infer_device(self._h, q.data_ptr(), q.shape[0], p.data_ptr(), _stream(q)))
+        return p
+
+    def parameters(self) -> np.ndarray:
+        out = np.zeros(lib.vg_mlp_param_count(self.robot.dimension()), np.float32)
+        check(lib.vg_mlp_get_params(self._h, _ptr(out)))
+        return out
+
+    def load_parameters(self, params) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        if p.size != lib.vg_mlp_param_count(self.robot.dimension()):
+            raise ValueError("parameter count does not match this robot's network")
+        check(lib.vg_mlp_set_params(self._h, _ptr(p)))
+
+    def validate_motion_batch(self, starts, goals, environment: Environment, resolution: int | None = None,
+                              probes: int = 8, out=None, blocks=None):
+        """Edge verdicts (those of Robot.validate_motion_batch) with each edge's blocks checked
+        in the order the network ranks them."""
+        import torch
+
+        res = self.robot.resolution() if resolution is None else int(resolution)
+        a, b = starts.contiguous(), goals.contiguous()
+        out = torch.empty(a.shape[0], dtype=torch.uint8, device=a.device) if out is None else out
+        bp = blocks.data_ptr() if blocks is not None else None
+        check(lib.vg_validate_motions_learned_device(self.robot.name.encode(), environment.handle, self._h, a.data_ptr(),
+                                                     b.data_ptr(), a.shape[0], res, probes, out.data_ptr(), bp,
+                                                     _stream(a)))
+        return out
+
+
+class Batch:
+    """Edge checks of several robots / environments recorded once and replayed as one CUDA graph
+    (vg_batch): refill the same tensors, then call launch()."""
+
+    def __init__(self):
+        self._h = lib.vg_batch_create()
+        self._keep = []  # tensors, environments and predictors the graph refers to
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.vg_batch_destroy(h)
+            self._h = None
+
+    def add(self, robot: Robot, environment: Environment, starts, goals, out, resolution: int | None = None,
+            predictor: CollisionPredictor | None = None, probes: int = 8, blocks=None) -> None:
+        res = robot.resolution() if resolution is None else int(resolution)
+        a, b = starts.contiguous(), goals.contiguous()
+        self._keep += [a, b, out, environment, predictor, blocks]
+        check(lib.vg_batch_add_motions(self._h, robot.name.encode(), environment.handle, a.data_ptr(), b.data_ptr(),
+                                       a.shape[0], res, predictor.handle if predictor else None,
+                                       probes if predictor else 0, out.data_ptr(),
+                                       blocks.data_ptr() if blocks is not None else None))
+
+    def launch(self, stream=None) -> None:
+        import torch
+
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        check(lib.vg_batch_launch(self._h, s))
