@@ -62,6 +62,9 @@ def _defines() -> list[str]:
         out.append("-DVG_STAGED_ALL")
     # VG_CAPT_SHARED_WEIGHT=w: the pointcloud query scans one lane's list with the whole warp
     # when 4 x the longest list exceeds w x the warp's shared steps
+    # VG_DEFAULT_LOOPED_ENV=1: the default edge kernel runs the environment section as loops
+    if os.environ.get("VG_DEFAULT_LOOPED_ENV") == "1":
+        out.append("-DVG_DEFAULT_LOOPED_ENV=1")
     w = os.environ.get("VG_CAPT_SHARED_WEIGHT")
     if w:
         out.append(f"-DVG_CAPT_SHARED_WEIGHT={int(w)}")

@@ -23,6 +23,11 @@
 #ifndef VG_MIN_BLOCKS_WIDE
 #define VG_MIN_BLOCKS_WIDE 3
 #endif
+// Environment section form of the default same-edge kernel: 0 unrolled, 1 loops (the
+// register-rich variant and the states kernel always use loops).
+#ifndef VG_DEFAULT_LOOPED_ENV
+#define VG_DEFAULT_LOOPED_ENV 0
+#endif
 
 namespace vg
 {
@@ -344,7 +349,7 @@ namespace vg
     // (block i = block 0 minus v / (W n), i times).  The edge is invalid if any checked block is,
     // and the reference would have stopped at the first invalid block, so the block count
     // reported is that block's index + 1.
-    template <typename Robot, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = false>
+    template <typename Robot, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = VG_DEFAULT_LOOPED_ENV != 0>
     __global__ void __launch_bounds__(128, kMinBlocks) edges_grouped_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];

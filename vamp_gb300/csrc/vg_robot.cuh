@@ -20,7 +20,7 @@ namespace vg
         return cudaGetLastError();
     }
 
-    template <typename R, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = false>
+    template <typename R, int W, bool kLearned, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = VG_DEFAULT_LOOPED_ENV != 0>
     cudaError_t launch_edges_grouped(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
         edges_grouped_kernel<R, W, kLearned, kMinBlocks, kLoopedEnv><<<grid, block, smem, s>>>(p);
