@@ -86,3 +86,23 @@ def test_danger_boxes_hold_just_outside_their_edges(port):
                 assert d > margin, (chk["links"], pi, q, d)
                 tested += 1
     assert tested > 1000
+
+
+@pytest.mark.parametrize("robot", ROBOTS)
+def test_containing_spheres_hold_every_fine_sphere(port, robot):
+    """The self checks skip a row of fine pairs when A's sphere misses B's containing sphere: it
+    must contain each of B's fine spheres with the margin, at any configuration."""
+    from vamp_gb300.robotgen.codegen import CONTAIN_MARGIN, Kin, containing_radius, slot_table
+
+    m = model(robot)
+    kin = Kin(m)
+    slots, cslot = slot_table(m)
+    rb = port.robot(robot)
+    rng = np.random.default_rng(3)
+    for q in np.array(m["s_a"]) + rng.random((20, len(m["s_a"]))) * np.array(m["s_m"]):
+        s = rb.spheres_f64(q)
+        for e in m["env_checks"]:
+            c = s[cslot[e["link"]], :3]
+            R = containing_radius(m, kin, e) + CONTAIN_MARGIN
+            for f in e["fine"]:
+                assert np.linalg.norm(s[f, :3] - c) + s[f, 3] <= R - 0.9 * CONTAIN_MARGIN, (robot, e["link"], f)

@@ -426,6 +426,22 @@ def danger_boxes(model: dict, cull) -> tuple:
     return checks, pairs
 
 
+CONTAIN_MARGIN = 1e-4  # metres between a link's fine spheres and its containing sphere
+
+
+def containing_radius(model: dict, kin, env_check: dict) -> float:
+    """Largest |fine centre - coarse centre| + fine radius of a link, in float64."""
+    slots, cslot = slot_table(model)
+    link = env_check["link"]
+    fc, pc = kin.sphere_in_frame(slots[cslot[link]][0], slots[cslot[link]][1])
+    best = 0.0
+    for f in env_check["fine"]:
+        ff, pf = kin.sphere_in_frame(slots[f][0], slots[f][1])
+        assert ff == fc, "a link's fine spheres and its coarse sphere share one frame"
+        best = max(best, float(np.linalg.norm(np.asarray(pf, float) - np.asarray(pc, float))) + float(slots[f][2]))
+    return best
+
+
 def load_cull(name: str):
     """Live fine self pairs per self check (None: all live), from robots/<name>.cull.json."""
     path = MODELS / f"{name}.cull.json"
@@ -636,6 +652,9 @@ def gen_cuda(model: dict) -> str:
             w(f"    __constant__ int4 {pre}SelfA[{len(rows_a)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_a)}}};")
             w(f"    __constant__ int4 {pre}SelfB[{len(rows_b)}] = {{{', '.join('{%d, %d, %d, %d}' % r for r in rows_b)}}};")
             w(f"    __constant__ float {pre}CoarseR[{len(lay['coarse'])}] = {{{', '.join(lit32(model['coarse_spheres'][model['env_checks'][k]['link']]['r']) for k in lay['coarse'])}}};")
+            w(f"    // per environment-check link: radius about its coarse centre that contains every fine sphere")
+            w(f"    // of the link with {CONTAIN_MARGIN} m to spare (exact geometry, rounded up to FP32)")
+            w(f"    __constant__ float {pre}ContainR[{len(model['env_checks'])}] = {{{', '.join(lit32(f32_up(containing_radius(model, kin, e) + CONTAIN_MARGIN)) for e in model['env_checks'])}}};")
             cb_checks, cb_pairs = danger_boxes(model, cull1)
             box = lambda b: "{%s}" % ", ".join(lit32(v) for v in b)  # noqa: E731
             w(f"    // danger boxes (joint space, inside the widened limits): a live pair can come within the")
@@ -885,8 +904,9 @@ def gen_cuda(model: dict) -> str:
             out.append("    if (need)")
             out.append("    {")
             if staged:
-                out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
-                out.append(f"                                           : self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
+                cbc = f"make_float4(cs[{kb}].x, cs[{kb}].y, cs[{kb}].z, {pre}ContainR[{kb}])"
+                out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]}, {cbc})")
+                out.append(f"                                           : self_pairs(st, {sid[fa]}, {sid[fb]}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]}, {cbc});")
             else:
                 out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
                 out.append(f"                                           : self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
@@ -913,6 +933,7 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
     if (need)
     {{
         const int4 u = {pre}SelfB[c];
+        const float4 cbc = make_float4(cb[0], cb[vg::kStageStride], cb[2 * vg::kStageStride], {pre}ContainR[t.y]);
         unsigned acc = 0u;
         if (ctx.in_limits)
         {{
@@ -923,12 +944,12 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
             const bool in = (qa >= bx.x) & (qa <= bx.y) & (qb >= bx.z) & (qb <= bx.w);
             if (__any_sync(vg::kFull, in))
             {{
-                acc = self_pairs_boxed(st, t.z, t.w, u.x, u.y, jj.z, qa, qb);
+                acc = self_pairs_boxed(st, t.z, t.w, u.x, u.y, jj.z, qa, qb, cbc);
             }}
         }}
         else
         {{
-            acc = self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w);
+            acc = self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w, cbc);
         }}
         const unsigned hit = ctx.vote(acc, need);
         if (hit && !(ctx.alive &= ~hit)) return;
@@ -1073,11 +1094,23 @@ for (int k = 0; k < {n_env}; ++k)
 
     // OR of the sign bits of the fine self-collision tests of pairs[k0..k1) (slot ids), the first
     // slot of each pair in staged frame fa, the second in staged frame fb.
-    static __device__ __noinline__ unsigned self_pairs(const float *st, int fa, int fb, const int2 *pairs, int k0, int k1)
+    // A's fine sphere ca against B's containing sphere cbc (every fine sphere of B lies inside it
+    // with CONTAIN margin to spare): whether any lane's sphere may touch one of B's fine spheres.
+    // Where no lane's does, the pair tests of this sphere have clear sign bits and are skipped.
+    static __device__ __forceinline__ bool row_may_hit(const float4 ca, const float4 cbc)
+    {{
+        const float dx = __fsub_rn(ca.x, cbc.x), dy = __fsub_rn(ca.y, cbc.y), dz = __fsub_rn(ca.z, cbc.z);
+        const float rr = __fadd_rn(ca.w, cbc.w);
+        return __any_sync(vg::kFull, __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))) < __fmul_rn(rr, rr));
+    }}
+
+    static __device__ __noinline__ unsigned self_pairs(const float *st, int fa, int fb, const int2 *pairs, int k0, int k1,
+                                                       float4 cbc)
     {{
         const vg::Frame a = frame_at(st, fa), b = frame_at(st, fb);
         unsigned acc = 0u;
         int last = -1;
+        bool row = false;
         float4 ca = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll 1
         for (int k = k0; k < k1; ++k)
@@ -1087,6 +1120,11 @@ for (int k = 0; k < {n_env}; ++k)
             {{
                 ca = vg::frame_point(a, {pre}SlotOff[pr.x]);
                 last = pr.x;
+                row = row_may_hit(ca, cbc);
+            }}
+            if (!row)
+            {{
+                continue;
             }}
             const float4 cb = vg::frame_point(b, {pre}SlotOff[pr.y]);
             acc |= vg::self_bits(ca.x, ca.y, ca.z, cb.x, cb.y, cb.z, __fadd_rn(ca.w, cb.w));
@@ -1099,11 +1137,12 @@ for (int k = 0; k < {n_env}; ++k)
     // the check has no boxes): outside it the pair keeps the culling margin, so its test value
     // cannot be negative.  Warp-uniform; all 32 lanes call.
     static __device__ __noinline__ unsigned self_pairs_boxed(const float *st, int fa, int fb, int k0, int k1, int box0,
-                                                             float qa, float qb)
+                                                             float qa, float qb, float4 cbc)
     {{
         const vg::Frame a = frame_at(st, fa), b = frame_at(st, fb);
         unsigned acc = 0u;
         int last = -1;
+        bool row = false;
         float4 ca = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll 1
         for (int k = k0; k < k1; ++k)
@@ -1121,6 +1160,11 @@ for (int k = 0; k < {n_env}; ++k)
             {{
                 ca = vg::frame_point(a, {pre}SlotOff[pr.x]);
                 last = pr.x;
+                row = row_may_hit(ca, cbc);
+            }}
+            if (!row)
+            {{
+                continue;
             }}
             const float4 cb = vg::frame_point(b, {pre}SlotOff[pr.y]);
             acc |= vg::self_bits(ca.x, ca.y, ca.z, cb.x, cb.y, cb.z, __fadd_rn(ca.w, cb.w));
