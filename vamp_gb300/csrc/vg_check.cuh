@@ -430,16 +430,13 @@ namespace vg
         // blocks per step (a shared step also pays broadcasts and a vote: weighted by
         // VG_CAPT_SHARED_WEIGHT / 4)
         const uint32_t shared_steps = __reduce_add_sync(kFull, (len + 31u) >> 5);
-        // (the scans below take two blocks per lane and step; the choice compares the one-block
-        // step counts, which keeps their ratio)
         bool hit = false;
         if (4u * longest <= VG_CAPT_SHARED_WEIGHT * shared_steps)
         {
-            // two blocks per step: both loads in flight before either test
 #pragma unroll 1
-            for (uint32_t b = b0; b < b1 && !hit; b += 2u)
+            for (uint32_t b = b0; b < b1 && !hit; ++b)
             {
-                hit = capt_block(c, b, x, y, z, rc) | (b + 1u < b1 && capt_block(c, b + 1u, x, y, z, rc));
+                hit = capt_block(c, b, x, y, z, rc);
             }
         }
         else
@@ -454,13 +451,11 @@ namespace vg
                 const float qrc = __shfl_sync(kFull, rc, L);
                 const uint32_t s0 = __shfl_sync(kFull, b0, L), s1 = __shfl_sync(kFull, b1, L);
                 bool found = false;
-                // 64 blocks per step (two per lane, both loads in flight), one vote per step
 #pragma unroll 1
-                for (uint32_t base = s0; base < s1; base += 64u)
+                for (uint32_t base = s0; base < s1; base += 32u)
                 {
                     const uint32_t b = base + static_cast<uint32_t>(lane);
-                    const bool h = (b < s1 && capt_block(c, b, qx, qy, qz, qrc)) |
-                                   (b + 32u < s1 && capt_block(c, b + 32u, qx, qy, qz, qrc));
+                    const bool h = b < s1 && capt_block(c, b, qx, qy, qz, qrc);
                     if (__any_sync(kFull, h))
                     {
                         found = true;
