@@ -609,6 +609,9 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
         w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
         w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
+        env_of = {e["link"]: k for k, e in enumerate(model["env_checks"])}
+        w(f"    // per link pair: environment-check index of link A's and link B's coarse sphere")
+        w(f"    __constant__ int2 {pre}SelfEnvIdx[{len(self_rows)}] = {{{', '.join('{%d, %d}' % (env_of[e['links'][0]], env_of[e['links'][1]]) for e in model['self_checks'])}}};")
         w("#endif")
         cull = load_cull(name)
         live_start, live_pairs = [0], []
@@ -749,10 +752,13 @@ def gen_cuda(model: dict) -> str:
         float F[kFrames * 12];
         frames(q, F);
 {chr(10).join("        " + l for l in limits_code(model, load_cull(name)))}
+        // coarse centres, computed once: the self loop reads them for every link pair
+        float4 CC[{len(model['env_checks'])}];
 #pragma unroll 1
         for (int c = 0; c < {len(model['env_checks'])}; ++c)
         {{
             const float4 k = centre(F, {pre}EnvCoarse[c]);
+            CC[c] = k;
             unsigned need = ctx.env_hit(k.x, k.y, k.z, k.w, ctx.alive);
 #pragma unroll 1
             for (int i = {pre}EnvStart[c]; need && i < {pre}EnvStart[c + 1]; ++i)
@@ -770,7 +776,8 @@ def gen_cuda(model: dict) -> str:
         for (int c = 0; c < {len(self_rows)}; ++c)
         {{
             const int4 row = {pre}SelfRow[c];
-            const float4 a = centre(F, row.x), b = centre(F, row.y);
+            const int2 ce = {pre}SelfEnvIdx[c];
+            const float4 a = CC[ce.x], b = CC[ce.y];
             unsigned need = ctx.self_hit(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, ctx.alive);
             if (!need)
             {{
