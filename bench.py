@@ -309,6 +309,35 @@ def run_capt(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup}))
 
 
+def run_debug(args, world, rank, local):
+    """Debug reports (Robot::fkcc_debug) of 65,536 Panda configurations in the 60-primitive scene:
+    per fine sphere the objects it collides with, per fine self pair whether it collides."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    env = vg.Environment.from_scene(scenes.scene_config1(SCENE_SEED))
+    q = torch.from_numpy(scenes.configurations(vg.panda.s_m, vg.panda.s_a, N_EDGES, 91)).to(dev)
+    for _ in range(max(args.warmup, 3)):
+        vg.panda.debug_batch(q, env)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        bits, pairs = vg.panda.debug_batch(q, env)  # synchronous
+        ts.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.mean(ts))
+    if rank == 0:
+        print(json.dumps({"metric": "debug reports/s on 1 GB300 (Robot::fkcc_debug)", "value": N_EDGES / (ms / 1e3),
+                          "unit": "configurations/s", "ms_per_step": ms, "configurations": N_EDGES,
+                          "sphere_object_hits": int(torch.count_nonzero(bits).item()),
+                          "colliding_pairs": int(pairs.sum().item()), "steps": args.steps, "warmup": args.warmup,
+                          "timing": "wall clock of the synchronous call (scratch allocation included)"}))
+
+
 MIXED_ROBOTS = ("ur5", "fetch", "baxter", "panda")
 MIXED_EDGES = 16384
 
@@ -664,9 +693,9 @@ def main():
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
                          "2 warp per edge with the register-rich build")
-    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed"],
+    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
-                         "mixed: four robots in one CUDA graph")
+                         "mixed: four robots in one CUDA graph; debug: per-sphere collision reports")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
@@ -675,6 +704,8 @@ def main():
         run_capt(args, world, rank, local)
     elif args.workload == "mixed":
         run_mixed(args, world, rank, local)
+    elif args.workload == "debug":
+        run_debug(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

@@ -149,6 +149,21 @@ int vg_validate_motions(
     const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution, uint8_t *out);
 int vg_sphere_fk(const char *robot, const float *q, size_t n, float *out);
 
+/* ------------------------------------------------------------------------- debug reports
+ * Replaces Robot::fkcc_debug (robots/panda.hh:468), the per-sphere collision listing behind the
+ * Python binding's debug() (bindings/robot_helper.hh:249-253, 585-589), for a batch of
+ * configurations.  For each configuration: env_bits [fine][words], a bit per environment object
+ * a fine sphere collides with (sphere_environment_get_collisions' rule, collision/validity.hh:
+ * 152-249; pointclouds are not part of it), the bit index being the object's insertion order
+ * among the environment's primitives (the reference reports object names); pairs [self_pairs],
+ * 1 for each fine self pair that collides, pairs in the order of the robot's self checks (the
+ * reference's order; it reports the colliding pairs' sphere indices).  Sizes from
+ * vg_debug_sizes.  The device form is synchronous (it allocates and frees its scratch). */
+int vg_debug_sizes(const char *robot, const vg_env *env, int *fine, int *words, int *self_pairs);
+int vg_debug_device(const char *robot, vg_env *env, const float *q, size_t n, uint32_t *env_bits, uint8_t *pairs,
+                    void *stream);
+int vg_debug(const char *robot, vg_env *env, const float *q, size_t n, uint32_t *env_bits, uint8_t *pairs);
+
 /* ------------------------------------------------------------------- tensor-core GEMM
  * D[M][N] (fp32) = A[M][K] * B[N][K]^T with A, B row-major bf16 (device pointers), on the 5th-
  * generation tensor cores (tcgen05, FP32 accumulation in tensor memory).  M % 128 == 0,

@@ -55,6 +55,8 @@ static const int kStride[5] = {5, 9, 9, 16, 16};
 struct vgo_env
 {
     float *obj[5];
+    int *ids[5];  /* insertion order of each object over all kinds (0, 1, ...) */
+    int n_added;
     size_t n[5], cap[5];
     vgo_capt *clouds[VGO_MAX_CLOUDS];
     int n_clouds;
@@ -73,7 +75,10 @@ void vgo_env_destroy(vgo_env *e)
     if (!e)
         return;
     for (int k = 0; k < 5; ++k)
+    {
         free(e->obj[k]);
+        free(e->ids[k]);
+    }
     for (int i = 0; i < e->n_clouds; ++i)
         vgo_capt_destroy(e->clouds[i]);
     free(e);
@@ -93,14 +98,17 @@ static void env_insert(vgo_env *e, int kind, const float *f)
     {
         e->cap[kind] = e->cap[kind] ? 2 * e->cap[kind] : 16;
         e->obj[kind] = (float *)realloc(e->obj[kind], e->cap[kind] * s * sizeof(float));
+        e->ids[kind] = (int *)realloc(e->ids[kind], e->cap[kind] * sizeof(int));
     }
     size_t pos = e->n[kind];
     while (pos > 0 && e->obj[kind][(pos - 1) * s + s - 1] > f[s - 1])
     {
         memcpy(e->obj[kind] + pos * s, e->obj[kind] + (pos - 1) * s, s * sizeof(float));
+        e->ids[kind][pos] = e->ids[kind][pos - 1];
         --pos;
     }
     memcpy(e->obj[kind] + pos * s, f, s * sizeof(float));
+    e->ids[kind][pos] = e->n_added++;
     e->n[kind]++;
 }
 
@@ -288,6 +296,39 @@ int vgo_sphere_env(const vgo_env *e, int lanes, const float *x, const float *y, 
     return 0;
 }
 
+int vgo_env_total(const vgo_env *e)
+{
+    return e->n_added;
+}
+
+/* sphere_environment_get_collisions (collision/validity.hh:152-249) for one sphere: per kind, the
+ * objects in min_distance order until min_distance - max_extent has a clear sign bit; each one
+ * whose test value has its sign bit set is reported (bit = the object's insertion id).
+ * Pointclouds are not part of it. */
+static void debug_sphere(const vgo_env *e, float x, float y, float z, float r, uint32_t *bits)
+{
+    const float v = fmaf(x, x, fmaf(z, z, y * y));
+    const float rsq = r * r;
+#define VGO_DEBUG_KIND(KIND, TEST, ARG)                                                           \
+    for (size_t i = 0; i < e->n[KIND]; ++i)                                                       \
+    {                                                                                             \
+        const float *o = e->obj[KIND] + i * kStride[KIND];                                        \
+        if (vgo_lane_breaks(o[kStride[KIND] - 1], v, r, e->sqrt_mode))                            \
+            break;                                                                                \
+        if (vgo_signbit(TEST(o, x, y, z, ARG)))                                                   \
+        {                                                                                         \
+            const int id = e->ids[KIND][i];                                                       \
+            bits[id >> 5] |= 1u << (id & 31);                                                     \
+        }                                                                                         \
+    }
+    VGO_DEBUG_KIND(0, t_sphere, r)
+    VGO_DEBUG_KIND(1, t_capsule, r)
+    VGO_DEBUG_KIND(2, t_zcapsule, r)
+    VGO_DEBUG_KIND(3, t_cuboid, rsq)
+    VGO_DEBUG_KIND(4, t_zcuboid, rsq)
+#undef VGO_DEBUG_KIND
+}
+
 const struct vgo_capt *vgo_env_capt(const vgo_env *e, int idx)
 {
     return (idx >= 0 && idx < e->n_clouds) ? e->clouds[idx] : NULL;
@@ -338,6 +379,31 @@ int vgo_robot_dim(const vgo_robot *r) { return r->dim; }
 int vgo_robot_slots(const vgo_robot *r) { return r->slots; }
 int vgo_robot_fine(const vgo_robot *r) { return r->fine; }
 int vgo_robot_resolution(const vgo_robot *r) { return r->resolution; }
+
+int vgo_robot_self_pairs(const vgo_robot *r)
+{
+    return r->self_start[r->n_self];
+}
+
+/* Robot::fkcc_debug (robots/panda.hh:468-...) for one configuration: for each fine sphere the
+ * environment objects it collides with (sphere_environment_get_collisions), and for every fine
+ * self pair of every self check, in the reference's order, whether it collides
+ * (sphere_sphere_self_collision, collision/validity.hh:23-44).  env_words is [fine][words]. */
+void vgo_debug(const vgo_robot *r, const vgo_env *e, const float *q, uint32_t *env_words, int words, uint8_t *pairs)
+{
+    float s[4 * VGO_MAX_SLOTS];
+    r->f32(q, s);
+    memset(env_words, 0, sizeof(uint32_t) * (size_t)words * (size_t)r->fine);
+    for (int i = 0; i < r->fine; ++i)
+        debug_sphere(e, s[4 * i], s[4 * i + 1], s[4 * i + 2], s[4 * i + 3], env_words + (size_t)i * words);
+    const int np = vgo_robot_self_pairs(r);
+    for (int p = 0; p < np; ++p)
+    {
+        const float *a = s + 4 * r->self_fine[2 * p], *b = s + 4 * r->self_fine[2 * p + 1];
+        const float rs = a[3] + b[3];
+        pairs[p] = (uint8_t)vgo_signbit(fmaf(-rs, rs, sql2(a[0], a[1], a[2], b[0], b[1], b[2])));
+    }
+}
 
 void vgo_robot_limits(const vgo_robot *r, float *s_m, float *s_a)
 {

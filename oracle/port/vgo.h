@@ -51,6 +51,13 @@ void vgo_robot_limits(const vgo_robot *r, float *s_m, float *s_a);
 void vgo_robot_spheres_f32(const vgo_robot *r, const float *q, float *out);
 void vgo_robot_spheres_f64(const vgo_robot *r, const double *q, double *out);
 
+/* objects added so far (insertion ids run 0 .. total-1 over all kinds) */
+int vgo_env_total(const vgo_env *e);
+/* fine self pairs over all self checks */
+int vgo_robot_self_pairs(const vgo_robot *r);
+/* Robot::fkcc_debug for one configuration: env_words [fine][words] (bit = insertion id of an
+ * object the sphere collides with), pairs [self pairs] (1 = the fine pair collides) */
+void vgo_debug(const vgo_robot *r, const vgo_env *e, const float *q, uint32_t *env_words, int words, uint8_t *pairs);
 /* ------------------------------------------------------------------------------------- queries */
 /* sphere_environment_in_collision over one block of `lanes` spheres (validity.hh:47-150) */
 int vgo_sphere_env(const vgo_env *e, int lanes, const float *x, const float *y, const float *z, const float *r);

@@ -17,6 +17,7 @@ struct RefEnv
     vamp::collision::Environment<float> scalar;
     std::unique_ptr<vamp::collision::Environment<vamp::FloatVector<vamp::FloatVectorWidth>>> vec;
     bool dirty = true;
+    int n_added = 0;  // objects are named by their insertion order ("0", "1", ...)
 
     void finalize()
     {

@@ -10,6 +10,8 @@
 //   FloatVector<8>::sqrt (rsqrt based on x86)                     vector/avx.hh:412-415
 #include "ref_common.hh"
 
+#include <string>
+
 #include <cstring>
 
 using namespace vamp;
@@ -31,6 +33,7 @@ void vgref_env_add_sphere(void *h, const float *f)
 {
     auto *e = static_cast<RefEnv *>(h);
     e->scalar.spheres.emplace_back(Sphere<float>(f[0], f[1], f[2], f[3]));
+    e->scalar.spheres.back().name = std::to_string(e->n_added++);
     e->dirty = true;
 }
 
@@ -39,6 +42,7 @@ void vgref_env_add_capsule(void *h, const float *f, int z_aligned)
 {
     auto *e = static_cast<RefEnv *>(h);
     Capsule<float> c(f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7]);
+    c.name = std::to_string(e->n_added++);
     if (z_aligned)
     {
         e->scalar.z_aligned_capsules.emplace_back(c);
@@ -56,6 +60,7 @@ void vgref_env_add_cuboid(void *h, const float *f, int z_aligned)
     auto *e = static_cast<RefEnv *>(h);
     Cuboid<float> c(
         f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9], f[10], f[11], f[12], f[13], f[14]);
+    c.name = std::to_string(e->n_added++);
     if (z_aligned)
     {
         e->scalar.z_aligned_cuboids.emplace_back(c);

@@ -12,6 +12,7 @@
 
 #include <atomic>
 #include <cstring>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -181,6 +182,44 @@ int VG_FN(_fkcc_block)(void *env, const float *q)
         block[j] = FloatVector<kRake>(row);
     }
     return Robot::fkcc<kRake>(*e->vec, block) ? 1 : 0;
+}
+
+// Robot::fkcc_debug (robots/panda.hh:468) on one configuration broadcast to every lane, as the
+// Python binding's debug() calls it (bindings/robot_helper.hh:249-253).  env_words [fine][words]
+// gets a bit per reported object (objects are named by insertion order); the colliding fine self
+// pairs are written to pairs_ij (up to cap pairs), their count to *n_pairs.
+void VG_FN(_debug)(void *env, const float *q, uint32_t *env_words, int words, int *pairs_ij, int cap, int *n_pairs)
+{
+    auto *e = static_cast<RefEnv *>(env);
+    e->finalize();
+    Block block;
+    for (std::size_t j = 0; j < Robot::dimension; ++j)
+    {
+        std::array<float, kRake> row;
+        row.fill(q[j]);
+        block[j] = FloatVector<kRake>(row);
+    }
+    const auto out = Robot::fkcc_debug<kRake>(*e->vec, block);
+    std::memset(env_words, 0, sizeof(uint32_t) * words * out.first.size());
+    for (std::size_t i = 0; i < out.first.size(); ++i)
+    {
+        for (const auto &name : out.first[i])
+        {
+            const int id = std::stoi(name);
+            env_words[i * words + id / 32] |= 1u << (id % 32);
+        }
+    }
+    int k = 0;
+    for (const auto &pr : out.second)
+    {
+        if (k < cap)
+        {
+            pairs_ij[2 * k] = static_cast<int>(pr.first);
+            pairs_ij[2 * k + 1] = static_cast<int>(pr.second);
+        }
+        ++k;
+    }
+    *n_pairs = k;
 }
 
 // Per-state validity as the Python binding's validate() computes it: validate_motion(q, q) with

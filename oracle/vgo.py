@@ -137,6 +137,9 @@ class Port:
         lib.vgo_capt_build.restype = ctypes.POINTER(_Capt)
         lib.vgo_capt_destroy.argtypes = [ctypes.POINTER(_Capt)]
         lib.vgo_validate_motions_counted.argtypes = [_p, _p, ctypes.c_int, _p, _p, _sz, ctypes.c_int, _p, _p]
+        lib.vgo_env_total.argtypes = [_p]
+        lib.vgo_robot_self_pairs.argtypes = [_p]
+        lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
         self.lib = lib
 
     def sqrt_x86(self, v: np.ndarray) -> np.ndarray:
@@ -267,6 +270,18 @@ class PortEnv:
             raise IndexError(idx)
         return capt_layout(h.contents)
 
+    def debug(self, robot: PortRobot, q: np.ndarray):
+        """Robot::fkcc_debug per configuration: (env bits [n][fine][words] uint32 over insertion
+        ids, self pair flags [n][pairs] uint8)."""
+        q = np.ascontiguousarray(q, np.float32).reshape(-1, robot.dim)
+        words = max(1, (self.port.lib.vgo_env_total(self.h) + 31) // 32)
+        np_ = self.port.lib.vgo_robot_self_pairs(robot.h)
+        env_bits = np.zeros((len(q), robot.fine, words), np.uint32)
+        pairs = np.zeros((len(q), np_), np.uint8)
+        for i in range(len(q)):
+            self.port.lib.vgo_debug(robot.h, self.h, _ptr(q[i]), _ptr(env_bits[i]), words, _ptr(pairs[i]))
+        return env_bits, pairs
+
     def contact_distance(self, robot: PortRobot, q) -> float:
         q = np.ascontiguousarray(q, np.float64)
         return self.port.lib.vgo_contact_distance_f64(robot.h, self.h, _ptr(q))
@@ -307,6 +322,7 @@ class Reference:
             getattr(lib, f"vgref_{r}_motion_blocks").argtypes = [_p, _p, ctypes.c_int, _p, _sz, ctypes.c_long]
             getattr(lib, f"vgref_{r}_motion_blocks").restype = ctypes.c_long
             getattr(lib, f"vgref_{r}_sphere_fk").argtypes = [_p, _p]
+            getattr(lib, f"vgref_{r}_debug").argtypes = [_p, _p, _p, ctypes.c_int, _p, ctypes.c_int, _p]
         self.lib = lib
 
     def env(self, scene):
@@ -372,6 +388,22 @@ class RefEnv:
         for i in range(n):
             lib.vgref_env_get(self.h, kind, i, _ptr(out[i]))
         return out
+
+    def debug(self, robot: str, q: np.ndarray, n_fine: int, n_objects: int):
+        """Robot::fkcc_debug per configuration: (env bits [n][fine][words] over insertion ids,
+        list per configuration of the colliding fine pairs (i, j) in the reference's order)."""
+        q = np.ascontiguousarray(q, np.float32).reshape(len(q), -1)
+        words = max(1, (n_objects + 31) // 32)
+        bits = np.zeros((len(q), n_fine, words), np.uint32)
+        out_pairs = []
+        cap = 8192
+        buf = np.zeros(2 * cap, np.int32)
+        cnt = ctypes.c_int()
+        fn = getattr(self.ref.lib, f"vgref_{robot}_debug")
+        for i in range(len(q)):
+            fn(self.h, _ptr(q[i]), _ptr(bits[i]), words, _ptr(buf), cap, ctypes.byref(cnt))
+            out_pairs.append([(int(buf[2 * k]), int(buf[2 * k + 1])) for k in range(min(cnt.value, cap))])
+        return bits, out_pairs
 
     def validate_states(self, robot: str, q, threads: int = 1):
         q = np.ascontiguousarray(q, np.float32)

@@ -139,6 +139,22 @@ def main():
     np.savez_compressed(OUT / "cloud_panda.npz", points=cloud, r=np.array([0.012, 0.08, scenes.POINT_RADIUS], np.float32),
                         q=q, state_verdict=sv, a=ea, b=eb, edge_verdict=ev)
 
+    # --- per-sphere collision reports (Robot::fkcc_debug, robots/panda.hh:468; the binding's debug())
+    from vamp_gb300.robots import model as robot_model
+
+    for r, scene, seed in (("panda", scenes.scene_config0(3), 71), ("baxter", scenes.scene_config1(3), 72)):
+        rb = port.robot(r)
+        q = scenes.configurations(rb.s_m, rb.s_a, 256, seed)
+        renv = ref.env(scene)
+        n_obj = len(scene["spheres"]) + len(scene["capsules"]) + len(scene["cuboids"])
+        bits, pair_lists = renv.debug(r, q, rb.fine, n_obj)
+        order = {tuple(p): i for i, p in enumerate(p for e in robot_model(r)["self_checks"] for p in e["fine"])}
+        pairs = np.zeros((len(q), len(order)), np.uint8)
+        for i, lst in enumerate(pair_lists):
+            for pr in lst:
+                pairs[i, order[pr]] = 1
+        np.savez_compressed(OUT / f"debug_{r}.npz", q=q, env_bits=bits, pairs=pairs, **scene_arrays(scene))
+
     print("golden fixtures written to", OUT)
 
 

@@ -143,3 +143,15 @@ def test_library_capt_layout_is_the_reference_bit_for_bit(port):
     mine, ref = env.pointcloud_layout(0), port.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS)
     for k in ("tests", "aabbs", "aff_starts", "aff", "top"):
         assert np.array_equal(mine[k], ref[k], equal_nan=True), k
+
+
+@pytest.mark.parametrize("robot", ["panda", "baxter"])
+def test_debug_reports_match_the_reference(port, robot):
+    """Robot::fkcc_debug: per fine sphere the objects it collides with, per fine self pair
+    whether it collides (golden fixture from the compiled reference)."""
+    g = golden(f"debug_{robot}")
+    env = port.env(scene_of(g))
+    bits, pairs = env.debug(port.robot(robot), g["q"])
+    assert np.array_equal(bits, g["env_bits"])
+    assert np.array_equal(pairs, g["pairs"])
+    assert g["env_bits"].any() and g["pairs"].any()

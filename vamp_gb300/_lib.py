@@ -70,6 +70,9 @@ def _load() -> ctypes.CDLL:
         "vg_validate_motions_scored_device": ([_s, _p, _p, _p, _sz, _i, _p, _i, _p, _p, _p], _i),
         "vg_validate_motions_learned_device": ([_s, _p, _p, _p, _p, _sz, _i, _i, _p, _p, _p], _i),
         "vg_autotune_motions": ([_s, _p, _p, _p, _sz, _i, _p, _p, _p, _p], _i),
+        "vg_debug_sizes": ([_s, _p, _p, _p, _p], _i),
+        "vg_debug_device": ([_s, _p, _p, _sz, _p, _p, _p], _i),
+        "vg_debug": ([_s, _p, _p, _sz, _p, _p], _i),
         "vg_batch_create": ([], _p),
         "vg_batch_destroy": ([_p], None),
         "vg_batch_add_motions": ([_p, _s, _p, _p, _p, _sz, _i, _p, _i, _p, _p], _i),
@@ -132,6 +135,9 @@ EXPORTED = (
     "vg_validate_motions_scored_device",
     "vg_validate_motions_learned_device",
     "vg_autotune_motions",
+    "vg_debug_sizes",
+    "vg_debug_device",
+    "vg_debug",
     "vg_batch_create",
     "vg_batch_destroy",
     "vg_batch_add_motions",

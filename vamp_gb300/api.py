@@ -238,6 +238,40 @@ class Robot:
         check(lib.vg_validate_motions(self._b, environment.handle, _ptr(a), _ptr(b), len(a), res, _ptr(out)))
         return out
 
+    def debug(self, configuration, environment: Environment):
+        """Which objects each fine sphere collides with and which fine self pairs collide, for one
+        configuration (the reference binding's debug(), bindings/robot_helper.hh:249-253): a list
+        per fine sphere of object insertion indices (the reference lists object names), and the
+        colliding fine pairs (i, j)."""
+        bits, pairs = self.debug_batch(np.asarray(configuration, np.float32).reshape(1, self._dim), environment)
+        objs = [[w * 32 + b for w in range(bits.shape[2]) for b in range(32) if (int(bits[0, i, w]) >> b) & 1]
+                for i in range(bits.shape[1])]
+        from .robots import model
+
+        order = [tuple(p) for e in model(self.name)["self_checks"] for p in e["fine"]]
+        return objs, [order[k] for k in np.nonzero(pairs[0])[0]]
+
+    def debug_batch(self, configurations, environment: Environment):
+        """Debug reports of many configurations: (bits [n][fine][words] uint32 over object
+        insertion indices, pair flags [n][self pairs] uint8 in the order of the self checks)."""
+        fine, words, npairs = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib.vg_debug_sizes(self._b, environment.handle, ctypes.byref(fine), ctypes.byref(words), ctypes.byref(npairs)))
+        if _is_cuda_tensor(configurations):
+            import torch
+
+            q = configurations.contiguous()
+            n = q.shape[0]
+            bits = torch.empty((n, fine.value, words.value), dtype=torch.int32, device=q.device)
+            pairs = torch.empty((n, npairs.value), dtype=torch.uint8, device=q.device)
+            check(lib.vg_debug_device(self._b, environment.handle, q.data_ptr(), n, bits.data_ptr(), pairs.data_ptr(),
+                                      torch.cuda.current_stream(q.device).cuda_stream))
+            return bits, pairs
+        q = np.ascontiguousarray(configurations, np.float32).reshape(-1, self._dim)
+        bits = np.zeros((len(q), fine.value, words.value), np.uint32)
+        pairs = np.zeros((len(q), npairs.value), np.uint8)
+        check(lib.vg_debug(self._b, environment.handle, _ptr(q), len(q), _ptr(bits), _ptr(pairs)))
+        return bits, pairs
+
     def fk_slots(self, configurations) -> np.ndarray:
         """Every sphere slot (fine spheres, then each checked link's coarse sphere) [n, slots, 4]."""
         q = np.ascontiguousarray(configurations, np.float32).reshape(-1, self._dim)

@@ -66,18 +66,25 @@ namespace vg
         return std::sqrt(std::fma(z, z, std::fma(x, x, y * y)));
     }
 
-    static void insert_sorted(std::vector<float> &v, int width, const float *row)
+    // Inserts an object of a kind into the environment's sorted rows (`width` fields +
+    // min_distance; ascending min_distance, ties after existing) and its insertion id (the
+    // object's position among all objects added, any kind) into the parallel id list.
+    static void insert_sorted(vg_env *env, int kind, int width, const float *row)
     {
-        // rows are `width` fields + min_distance; keep ascending min_distance, ties after existing
+        std::vector<float> &v = env->obj[kind];
+        std::vector<int> &ids = env->ids[kind];
         const int w = width + 1;
         size_t pos = v.size() / w;
         v.resize(v.size() + w);
+        ids.resize(ids.size() + 1);
         while (pos > 0 && v[(pos - 1) * w + width] > row[width])
         {
             std::memcpy(&v[pos * w], &v[(pos - 1) * w], sizeof(float) * w);
+            ids[pos] = ids[pos - 1];
             --pos;
         }
         std::memcpy(&v[pos * w], row, sizeof(float) * w);
+        ids[pos] = env->n_added++;
     }
 
     // Sphere::min_distance (collision/shapes.hh:236-240)
@@ -483,7 +490,7 @@ int vg_env_add_sphere(vg_env *env, const float *f)
         return set_error(VG_ERR_ARG, "vg_env_add_sphere: null argument");
     float row[5] = {f[0], f[1], f[2], f[3], 0.0f};
     row[4] = sphere_min_distance(f);
-    insert_sorted(env->obj[0], 4, row);
+    insert_sorted(env, 0, 4, row);
     env->dirty = true;
     return VG_OK;
 }
@@ -495,7 +502,7 @@ int vg_env_add_capsule(vg_env *env, const float *f)
     float row[9];
     std::memcpy(row, f, sizeof(float) * 8);
     row[8] = capsule_min_distance(f);
-    insert_sorted(env->obj[(f[3] == 0.0f && f[4] == 0.0f) ? 2 : 1], 8, row);
+    insert_sorted(env, (f[3] == 0.0f && f[4] == 0.0f) ? 2 : 1, 8, row);
     env->dirty = true;
     return VG_OK;
 }
@@ -507,7 +514,7 @@ int vg_env_add_cuboid(vg_env *env, const float *f)
     float row[16];
     std::memcpy(row, f, sizeof(float) * 15);
     row[15] = cuboid_min_distance(f);
-    insert_sorted(env->obj[f[11] == 1.0f ? 4 : 3], 15, row);
+    insert_sorted(env, f[11] == 1.0f ? 4 : 3, 15, row);
     env->dirty = true;
     return VG_OK;
 }

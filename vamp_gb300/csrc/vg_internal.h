@@ -36,6 +36,9 @@ namespace vg
         const void *edges_learned_fn[2];
         int stage_floats;  // shared-memory staging floats per thread (after the environment image)
         cudaError_t (*spheres)(const float *, long long, float *, cudaStream_t);
+        // fkcc_debug's self part: flags [n][self_pairs] from sphere slots [n][slots][4]
+        cudaError_t (*debug_self)(const float *, long long, uint8_t *, cudaStream_t);
+        int self_pairs;  // fine pairs over all self checks
     };
 
     const RobotOps *find_robot(const char *name);
@@ -74,6 +77,8 @@ struct vg_env
 {
     // host copies, sorted by min_distance; each row: fields then min_distance (oracle layout)
     std::vector<float> obj[5];
+    std::vector<int> ids[5];  // insertion id (0, 1, ... over all kinds) of each row of obj
+    int n_added = 0;
     int lanes = 8;
     int sqrt_mode = 0;
     int schedule = 1;  // 0: a segment per edge, 1: a warp per edge (consecutive blocks)

@@ -613,6 +613,31 @@ namespace vg
         }
     }
 
+    // ----------------------------------------------------------------------- debug reports
+    //
+    // Robot::fkcc_debug (robots/panda.hh:468) for a batch of configurations, from their sphere
+    // slots (spheres_kernel): per fine sphere the environment objects it collides with, by
+    // sphere_environment_get_collisions' rule (collision/validity.hh:152-249: per kind, objects in
+    // min_distance order until min_distance - max_extent has a clear sign bit; pointclouds are not
+    // part of it), and per fine self pair of every self check whether it collides.
+
+    // one thread per (configuration, fine self pair): 1 where sphere_sphere_self_collision
+    // (collision/validity.hh:23-44) reports the pair
+    template <typename Robot>
+    __global__ void debug_self_kernel(const float *spheres, long long n, uint8_t *out)
+    {
+        const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (t >= n * Robot::kSelfPairs)
+        {
+            return;
+        }
+        const long long c = t / Robot::kSelfPairs;
+        const int2 pr = Robot::self_pair(static_cast<int>(t - c * Robot::kSelfPairs));
+        const float *a = spheres + (c * Robot::kSlots + pr.x) * 4;
+        const float *b = spheres + (c * Robot::kSlots + pr.y) * 4;
+        out[t] = static_cast<uint8_t>(self_bits(a[0], a[1], a[2], b[0], b[1], b[2], __fadd_rn(a[3], b[3])) >> 31);
+    }
+
     // ----------------------------------------------------------------------------- spheres
 
     template <typename Robot>

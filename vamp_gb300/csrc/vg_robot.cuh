@@ -35,6 +35,18 @@ namespace vg
     }
 
     template <typename R>
+    cudaError_t launch_debug_self(const float *spheres, long long n, uint8_t *out, cudaStream_t s)
+    {
+        const long long t = n * R::kSelfPairs;
+        if (t <= 0)
+        {
+            return cudaSuccess;
+        }
+        debug_self_kernel<R><<<static_cast<unsigned>((t + 255) / 256), 256, 0, s>>>(spheres, n, out);
+        return cudaGetLastError();
+    }
+
+    template <typename R>
     cudaError_t launch_spheres(const float *q, long long n, float *out, cudaStream_t s)
     {
         if (n <= 0)
@@ -86,6 +98,8 @@ namespace vg
         o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true>);
         o.stage_floats = R::kStage;
         o.spheres = &launch_spheres<R>;
+        o.debug_self = &launch_debug_self<R>;
+        o.self_pairs = R::kSelfPairs;
         return o;
     }
 }  // namespace vg

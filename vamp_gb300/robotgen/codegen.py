@@ -623,6 +623,8 @@ def gen_cuda(model: dict) -> str:
         w(f"    __constant__ int {pre}LiveStart[{len(live_start)}] = {{{', '.join(map(str, live_start))}}};")
         w(f"    __constant__ int2 {pre}LivePair[{max(1, len(live_pairs))}] = {{{', '.join('{%d, %d}' % p for p in live_pairs) or '{0, 0}'}}};")
         all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
+        w(f"    // every fine self pair, in the reference's order (debug reports; global memory)")
+        w(f"    __device__ const int2 {pre}AllPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         w(stg_if)
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         if True:
@@ -679,6 +681,8 @@ def gen_cuda(model: dict) -> str:
     w("    static constexpr int kSlots = %d;" % len(slots))
     w("    static constexpr int kFrames = %d;" % (len(kin.frames) + 1))
     w("    static constexpr int kEnvChecks = %d;" % len(model["env_checks"]))
+    w("    static constexpr int kSelfPairs = %d;" % sum(len(e["fine"]) for e in model["self_checks"]))
+    w("    static __device__ __forceinline__ int2 self_pair(int i) { return k%sAllPair[i]; }" % S)
     lay = stage_layout(model, kin, load_cull(name))
     w("    // floats of shared-memory staging per thread (non-constant entries of the fine checks' frames)")
     w("#if defined(VG_FORM_COMPACT)%s" % (" || !defined(VG_STAGED_ALL)" if tabled else ""))
