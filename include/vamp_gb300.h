@@ -74,6 +74,12 @@ int vg_env_add_cuboid(vg_env *env, const float *fields15);
  * xyz is [n][3], n >= 2; queries pad sphere radii by r_point; the tree affords points for radii
  * up to r_max.  At most 4 pointclouds per environment. */
 int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point);
+/* The same tree as vg_env_add_pointcloud, built on the current GPU (no counterpart in the
+ * reference, whose CAPT is built on the host: collision/capt.hh:294-365): xyz is a device array
+ * [n][3] on that GPU; the call returns once the tree is built (synchronous on `stream`, a
+ * cudaStream_t or NULL).  The layout is bit-identical to the host build's. */
+int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point,
+                                 void *stream);
 /* The tree of the index-th pointcloud (collision/capt.hh:584-617): sizes = {nlog2, tests,
  * leaves, 8-point blocks}; then, if non-NULL, tests[tests], aabbs[leaves][6], aff_starts[leaves
  * + 1], aff[blocks][3][8] (x, y, z planes of each block), top[6].  Call with NULL arrays for the

@@ -105,6 +105,18 @@ class Environment:
         pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
         check(lib.vg_env_add_pointcloud(self._h, _ptr(pts), len(pts), float(r_min), float(r_max), float(r_point)))
 
+    def add_pointcloud_device(self, points, r_min: float, r_max: float, r_point: float) -> None:
+        """The same CAPT built on the GPU from a CUDA tensor of points [n, 3] (float32); the layout
+        is bit-identical to add_pointcloud's."""
+        import torch
+
+        pts = points.detach().to(torch.float32).reshape(-1, 3).contiguous()
+        if not pts.is_cuda:
+            raise ValueError("add_pointcloud_device takes a CUDA tensor")
+        with torch.cuda.device(pts.device):
+            check(lib.vg_env_add_pointcloud_device(self._h, pts.data_ptr(), pts.shape[0], float(r_min), float(r_max),
+                                                   float(r_point), _stream(pts)))
+
     def pointcloud_layout(self, index: int = 0) -> dict:
         sizes = np.zeros(4, np.uint64)
         nul = ctypes.c_void_p()

@@ -5,6 +5,7 @@
 // GPU and the oracle take identical early-exit decisions.
 #include "../../include/vamp_gb300.h"
 #include "vg_internal.h"
+#include "vg_capt_gpu.h"
 #include "x86_rsqrt_table.h"
 
 #include <cmath>
@@ -214,7 +215,7 @@ namespace vg
                 v.top[k] = c.top[k];
             v.r_point = c.r_point;
             v.nlog2 = c.nlog2;
-            v.n_tests = static_cast<int>(c.tests.size());
+            v.n_tests = static_cast<int>(c.n_tests());
             const size_t at = img.size();
             img.resize(at + sizeof(CaptView) / sizeof(float4));
             std::memcpy(&img[at], &v, sizeof(CaptView));
@@ -541,6 +542,45 @@ int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, 
     return VG_OK;
 }
 
+// Same tree as vg_env_add_pointcloud, built on the current GPU from device points xyz[n][3]
+// (synchronous on `stream`).  The environment must be used on this GPU.
+int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point,
+                                 void *stream)
+{
+    if (!env || !xyz || n < 2 || !(r_min >= 0.0f) || !(r_max >= r_min) || !(r_point >= 0.0f))
+        return set_error(VG_ERR_ARG, "vg_env_add_pointcloud_device: need at least 2 points and 0 <= r_min <= r_max, r_point >= 0");
+    if (env->clouds.size() >= static_cast<size_t>(kMaxClouds))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud_device: at most 4 pointclouds per environment");
+    if (n > (size_t{1} << 30))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud_device: at most 2^30 points");
+    int dev = 0;
+    VG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (env->device >= 0 && env->device != dev)
+        return set_error(VG_ERR_STATE, "vg_env_add_pointcloud_device: the environment lives on another device");
+    // earlier host-built clouds go up first, so that the device buffers stay in cloud order
+    if (int rc = upload_clouds(env))
+        return rc;
+    DeviceCapt d;
+    if (int rc = capt_build_device(xyz, n, r_min, r_max, r_point, static_cast<cudaStream_t>(stream), d))
+        return rc;
+    CaptHost c;
+    c.nlog2 = d.nlog2;
+    std::memcpy(c.top, d.top, sizeof(c.top));
+    c.r_min = r_min;
+    c.r_max = r_max;
+    c.r_point = r_point;
+    c.on_device = true;
+    c.device_blocks = d.blocks;
+    env->clouds.push_back(std::move(c));
+    env->d_clouds.push_back(d.tests);
+    env->d_clouds.push_back(d.aabbs);
+    env->d_clouds.push_back(d.starts);
+    env->d_clouds.push_back(d.aff);
+    env->device = dev;
+    env->dirty = true;
+    return VG_OK;
+}
+
 int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, float *tests, float *aabbs,
                              uint32_t *aff_starts, float *aff, float *top)
 {
@@ -548,9 +588,25 @@ int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, floa
         return set_error(VG_ERR_ARG, "vg_env_pointcloud_layout: bad argument");
     const CaptHost &c = env->clouds[index];
     sizes[0] = static_cast<uint64_t>(c.nlog2);
-    sizes[1] = c.tests.size();
-    sizes[2] = c.aabbs.size() / 6;
+    sizes[1] = c.n_tests();
+    sizes[2] = c.n_leaves();
     sizes[3] = c.blocks();
+    if (c.on_device)
+    {
+        // the arrays live on the GPU that built them
+        void *const *d = &env->d_clouds[4 * static_cast<size_t>(index)];
+        const size_t bytes[4] = {sizes[1] * sizeof(float), sizes[2] * 6 * sizeof(float), (sizes[2] + 1) * sizeof(uint32_t),
+                                 sizes[3] * 24 * sizeof(float)};
+        void *dst[4] = {tests, aabbs, aff_starts, aff};
+        for (int k = 0; k < 4; ++k)
+        {
+            if (dst[k] && bytes[k])
+                VG_CUDA(cudaMemcpy(dst[k], d[k], bytes[k], cudaMemcpyDeviceToHost), "vg_env_pointcloud_layout: copy");
+        }
+        if (top)
+            std::memcpy(top, c.top, sizeof(c.top));
+        return VG_OK;
+    }
     if (tests)
         std::memcpy(tests, c.tests.data(), c.tests.size() * sizeof(float));
     if (aabbs)

@@ -20,8 +20,13 @@ namespace vg
         std::vector<float> aff;             // blocks x 24: x[8], y[8], z[8]
         float top[6] = {0, 0, 0, 0, 0, 0};  // box of all finite points
         float r_min = 0, r_max = 0, r_point = 0;
+        // built on the GPU: the arrays exist only in device memory (sizes below)
+        bool on_device = false;
+        size_t device_blocks = 0;
 
-        size_t blocks() const { return aff.size() / 24; }
+        size_t blocks() const { return on_device ? device_blocks : aff.size() / 24; }
+        size_t n_tests() const { return on_device ? (size_t{1} << nlog2) - 1 : tests.size(); }
+        size_t n_leaves() const { return on_device ? size_t{1} << nlog2 : aabbs.size() / 6; }
     };
 
     // Returns false if there are fewer than 2 points.
