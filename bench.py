@@ -346,6 +346,56 @@ def run_debug(args, world, rank, local):
                           "timing": "wall clock of the synchronous call (scratch allocation included)"}))
 
 
+def run_filter(args, world, rank, local):
+    """Pointcloud filter (filter_pointcloud, collision/filter.hh:176-320) of 1,048,576 points on
+    the surfaces of 30 random cuboids and cylinders plus 2% noise, with the reference's Panda
+    settings (origin at the first joint, cull radius 1.19 m, filter radius 1 cm), then the CAPT
+    build of the kept points on the GPU.  The C oracle times the same filter on the host."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300.robots import model
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    m = model("panda")
+    org = np.array([0.0, 0.0, 0.333], np.float32)
+    rad, md = np.float32(1.19), 0.01
+    pts = scenes.surface_pointcloud(SCENE_SEED, 1 << 20)
+    d_pts = torch.from_numpy(pts).to(dev)
+    for _ in range(max(args.warmup, 3)):
+        kept = vg.filter_pointcloud_device(d_pts, md, rad, org, org - rad, org + rad, True)
+    ts, tb = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kept = vg.filter_pointcloud_device(d_pts, md, rad, org, org - rad, org + rad, True)  # synchronous
+        t1 = time.perf_counter()
+        vg.Environment().add_pointcloud_device(kept, m["min_radius"], m["max_radius"], scenes.POINT_RADIUS)
+        ts.append(t1 - t0)
+        tb.append(time.perf_counter() - t1)
+    host, ns = vg.filter_pointcloud(pts, md, rad, org, org - rad, org + rad, True)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle.vgo import Port
+
+        t0 = time.perf_counter()
+        want = Port().filter_pointcloud(pts, md, rad, org, org - rad, org + rad, True)
+        cpu = time.perf_counter() - t0
+        assert np.array_equal(want, host)
+    if rank == 0:
+        ms = 1e3 * float(np.median(ts))
+        print(json.dumps({
+            "metric": "pointcloud filter on 1 GB300 (filter_pointcloud)", "value": len(pts) / (ms / 1e3),
+            "unit": "points/s", "ms_per_step": ms, "points": len(pts), "kept": int(kept.shape[0]),
+            "capt_build_gpu_ms": 1e3 * float(np.median(tb)), "host_buffers_ms": ns / 1e6,
+            "cpu_baseline": None if cpu is None else {"value": len(pts) / cpu, "unit": "points/s", "cores": 1,
+                                                      "kind": "port", "sample": "the whole cloud, once"},
+            "steps": args.steps, "warmup": args.warmup,
+            "timing": "wall clock of the synchronous device call (allocation included)"}))
+
+
 MIXED_ROBOTS = ("ur5", "fetch", "baxter", "panda")
 MIXED_EDGES = 16384
 
@@ -701,9 +751,10 @@ def main():
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
                          "2 warp per edge with the register-rich build")
-    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug"],
+    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug", "filter"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
-                         "mixed: four robots in one CUDA graph; debug: per-sphere collision reports")
+                         "mixed: four robots in one CUDA graph; debug: per-sphere collision reports; "
+                         "filter: the pointcloud filter and CAPT build")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
@@ -714,6 +765,8 @@ def main():
         run_mixed(args, world, rank, local)
     elif args.workload == "debug":
         run_debug(args, world, rank, local)
+    elif args.workload == "filter":
+        run_filter(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

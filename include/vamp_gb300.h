@@ -80,6 +80,23 @@ int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, 
  * cudaStream_t or NULL).  The layout is bit-identical to the host build's. */
 int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point,
                                  void *stream);
+/* The reference's pointcloud filter on the current GPU (collision/filter.hh:176-320,
+ * filter_pointcloud; Python binding bindings/environment.cc:167-197): keeps a subset of xyz[n][3]
+ * in which no two consecutive points of six Morton-order passes lie within min_dist, and, when
+ * cull != 0, only points closer than max_range to origin[3] and inside the box workcell_min[3]
+ * .. workcell_max[3] (plus the reference's extra copy of point 0 when any point was culled).
+ * origin and the workcell are host arrays.  Equal Morton codes keep their previous order (the
+ * reference sorts with the unstable pdqsort; with a stable sort its results are these).  The
+ * kept points go to out (capacity n points), their number to *n_out.
+ *   _device: xyz and out on the current GPU; synchronous on `stream` (a cudaStream_t or NULL).
+ *   host form: xyz and out in host memory; *elapsed_ns (if non-NULL) gets the call's wall time,
+ *   as the reference's binding returns it. */
+int vg_filter_pointcloud_device(const float *xyz, size_t n, float min_dist, float max_range, const float *origin,
+                                const float *workcell_min, const float *workcell_max, int cull, float *out, size_t *n_out,
+                                void *stream);
+int vg_filter_pointcloud(const float *xyz, size_t n, float min_dist, float max_range, const float *origin,
+                         const float *workcell_min, const float *workcell_max, int cull, float *out, size_t *n_out,
+                         uint64_t *elapsed_ns);
 /* The tree of the index-th pointcloud (collision/capt.hh:584-617): sizes = {nlog2, tests,
  * leaves, 8-point blocks}; then, if non-NULL, tests[tests], aabbs[leaves][6], aff_starts[leaves
  * + 1], aff[blocks][3][8] (x, y, z planes of each block), top[6].  Call with NULL arrays for the

@@ -140,7 +140,22 @@ class Port:
         lib.vgo_env_total.argtypes = [_p]
         lib.vgo_robot_self_pairs.argtypes = [_p]
         lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
+        lib.vgo_filter_pointcloud.argtypes = [_p, _sz, _f, _f, _p, _p, _p, ctypes.c_int, _p]
+        lib.vgo_filter_pointcloud.restype = _sz
+        lib.vgo_filter_remap.argtypes = [_f, _f, _f]
+        lib.vgo_filter_remap.restype = ctypes.c_uint32
+        lib.vgo_morton.argtypes = [ctypes.c_uint32] * 3
+        lib.vgo_morton.restype = ctypes.c_uint32
         self.lib = lib
+
+    def filter_pointcloud(self, points, min_dist, max_range, origin, workcell_min, workcell_max, cull) -> np.ndarray:
+        """collision/filter.hh:176-278: the kept points, [m, 3]."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        o, lo, hi = (np.ascontiguousarray(v, np.float32) for v in (origin, workcell_min, workcell_max))
+        m = self.lib.vgo_filter_pointcloud(_ptr(pts), len(pts), min_dist, max_range, _ptr(o), _ptr(lo), _ptr(hi),
+                                           int(bool(cull)), _ptr(out))
+        return out[:m].copy()
 
     def sqrt_x86(self, v: np.ndarray) -> np.ndarray:
         return np.array([self.lib.vgo_sqrt_x86(float(x)) for x in np.asarray(v, np.float32)], np.float32)
@@ -323,10 +338,23 @@ class Reference:
             getattr(lib, f"vgref_{r}_motion_blocks").restype = ctypes.c_long
             getattr(lib, f"vgref_{r}_sphere_fk").argtypes = [_p, _p]
             getattr(lib, f"vgref_{r}_debug").argtypes = [_p, _p, _p, ctypes.c_int, _p, ctypes.c_int, _p]
+        lib.vgref_filter_pointcloud.argtypes = [_p, _sz, _f, _f, _p, _p, _p, ctypes.c_int, _p, _p]
+        lib.vgref_filter_remap.argtypes = [_f, _f, _f]
+        lib.vgref_filter_remap.restype = ctypes.c_uint
         self.lib = lib
 
     def env(self, scene):
         return RefEnv(self, scene)
+
+    def filter_pointcloud(self, points, min_dist, max_range, origin, workcell_min, workcell_max, cull) -> np.ndarray:
+        """The reference's filter_pointcloud (collision/filter.hh:176-320): the kept points, [m, 3]."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        m = _sz()
+        o, lo, hi = (np.ascontiguousarray(v, np.float32) for v in (origin, workcell_min, workcell_max))
+        self.lib.vgref_filter_pointcloud(_ptr(pts), len(pts), min_dist, max_range, _ptr(o), _ptr(lo), _ptr(hi),
+                                         int(bool(cull)), _ptr(out), ctypes.byref(m))
+        return out[: m.value].copy()
 
     def sphere_fk(self, robot: str, q: np.ndarray, n_spheres: int) -> np.ndarray:
         q = np.ascontiguousarray(q, np.float32)

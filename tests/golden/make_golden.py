@@ -35,14 +35,50 @@ def env_dump(env) -> dict:
     return {f"kind{k}": env.objects(k) for k in range(5)}
 
 
+def filter_cases() -> list:
+    """Inputs of the pointcloud filter fixtures: (points, min_dist, max_range, origin, workcell
+    min, workcell max, cull)."""
+    rng = np.random.default_rng(81)
+    org = np.array([0.0, 0.0, 0.333], np.float32)
+    surf = scenes.surface_pointcloud(82, n_points=4000)
+    uni = rng.uniform(-1.5, 1.5, (3000, 3)).astype(np.float32)
+    grid = (rng.integers(0, 30, (4000, 3)) * 0.02 - 0.3).astype(np.float32)  # repeated points and ties
+    far = (rng.uniform(-0.2, 0.2, (500, 3)) + 5.0).astype(np.float32)        # every point culled
+    mixed = np.concatenate([far[:50], surf[:2000]]).astype(np.float32)       # point 0 culled
+    box = lambda o, r: (o - r, o + r)  # noqa: E731
+    return [
+        (surf, 0.01, 1.19, org, *box(org, 1.19), True),
+        (surf, 0.03, 0.9, org, *box(org, 0.9), False),
+        (uni, 0.05, 0.6, org, *box(org, 0.6), False),  # points outside the mapping range
+        (grid, 0.021, 1.0, org, *box(org, 1.0), True),
+        (far, 0.01, 1.0, org, *box(org, 1.0), True),
+        (mixed, 0.015, 1.2, org, org - np.float32(1.2), org + np.float32(0.5), True),
+    ]
+
+
+def filter_fixtures(ref: Reference) -> None:
+    """The reference's filter_pointcloud (collision/filter.hh:176-320) on a few clouds."""
+    out = {}
+    for i, (pts, md, mr, o, lo, hi, cull) in enumerate(filter_cases()):
+        kept = ref.filter_pointcloud(pts, md, mr, o, lo, hi, cull)
+        out[f"points{i}"] = pts
+        out[f"params{i}"] = np.concatenate([[md, mr], o, lo, hi, [float(cull)]]).astype(np.float32)
+        out[f"kept{i}"] = kept
+    np.savez_compressed(OUT / "filter.npz", **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None)
+    ap.add_argument("--only", choices=["filter"], default=None, help="regenerate one group of fixtures")
     a = ap.parse_args()
     if build_reference(a.reference) is None:
         raise SystemExit("reference checkout not found (or not x86-64): cannot generate golden fixtures")
     ref = Reference()
     port = Port()
+    filter_fixtures(ref)
+    if a.only == "filter":
+        return
 
     # --- forward kinematics: fine sphere centres (Robot::sphere_fk)
     for r in ROBOTS:

@@ -155,3 +155,32 @@ def test_debug_reports_match_the_reference(port, robot):
     assert np.array_equal(bits, g["env_bits"])
     assert np.array_equal(pairs, g["pairs"])
     assert g["env_bits"].any() and g["pairs"].any()
+
+
+def _filter_case(g: dict, i: int):
+    p = g[f"params{i}"]
+    return g[f"points{i}"], float(p[0]), float(p[1]), p[2:5], p[5:8], p[8:11], bool(p[11])
+
+
+def test_filter_matches_the_reference(port):
+    """filter_pointcloud (collision/filter.hh:176-320): the restated filter keeps exactly the
+    reference's points, in its order (golden fixture from the compiled reference)."""
+    g = golden("filter")
+    for i in range(6):
+        pts, md, mr, o, lo, hi, cull = _filter_case(g, i)
+        kept = port.filter_pointcloud(pts, md, mr, o, lo, hi, cull)
+        assert kept.shape == g[f"kept{i}"].shape and np.array_equal(kept, g[f"kept{i}"]), i
+    assert len(g["kept4"]) == 1 and np.array_equal(g["kept4"][0], g["points4"][0])  # all culled: point 0 stays
+
+
+def test_filter_conversion_and_morton(port):
+    """remap_point's float -> uint32_t conversion and the Morton interleave (filter.hh:142-171)."""
+    lib = port.lib
+    assert lib.vgo_filter_remap(0.5, 0.0, 1.0) == 500
+    assert lib.vgo_filter_remap(-0.0005, 0.0, 1.0) == 0        # (-1, 0) truncates to 0
+    assert lib.vgo_filter_remap(-0.002, 0.0, 1.0) == 0xFFFFFFFF  # <= -1
+    assert lib.vgo_filter_remap(5e6, 0.0, 1.0) == 0xFFFFFFFF     # >= 2^32
+    assert lib.vgo_filter_remap(float("nan"), 0.0, 1.0) == 0xFFFFFFFF
+    assert lib.vgo_morton(1, 0, 0) == 1 and lib.vgo_morton(0, 1, 0) == 2 and lib.vgo_morton(0, 0, 1) == 4
+    assert lib.vgo_morton(0x7FF, 0, 0) == 0x49249249 and lib.vgo_morton(0, 0x7FF, 0) == 0x92492492
+    assert lib.vgo_morton(0, 0, 0x7FF) == 0x24924924  # z keeps 10 bits

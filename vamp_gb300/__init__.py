@@ -3,7 +3,8 @@
 The Python surface mirrors the reference's bindings (src/impl/vamp/bindings/robot_helper.hh and
 environment.cc): an `Environment` built from primitives, and one object per robot (`panda`,
 `ur5`, `fetch`, `baxter`) with `validate`, `validate_motion`, `fk`, `min_max_radii`,
-`dimension`, `resolution`, plus batched `validate_batch` / `validate_motion_batch`; and, with
+`dimension`, `resolution`, plus batched `validate_batch` / `validate_motion_batch`;
+`filter_pointcloud` (environment.cc:167-197) on the GPU; and, with
 no counterpart in the reference, `autotune`, `Batch` (checks replayed as one CUDA graph) and
 `CollisionPredictor` (the learned block ordering).
 
@@ -14,7 +15,7 @@ access raises ImportError (there is no CPU fallback).  Submodules that do not ne
 from __future__ import annotations
 
 _API = {"Environment", "Robot", "VampError", "SQRT_X86", "SQRT_EXACT", "panda", "ur5", "fetch", "baxter", "ROBOTS",
-        "autotune", "Batch", "CollisionPredictor", "SCHEDULES"}
+        "autotune", "Batch", "CollisionPredictor", "SCHEDULES", "filter_pointcloud", "filter_pointcloud_device"}
 
 
 def __getattr__(name):

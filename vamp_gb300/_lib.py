@@ -44,6 +44,8 @@ def _load() -> ctypes.CDLL:
         "vg_env_add_cuboid": ([_p, _p], _i),
         "vg_env_add_pointcloud": ([_p, _p, _sz, _f, _f, _f], _i),
         "vg_env_add_pointcloud_device": ([_p, _p, _sz, _f, _f, _f, _p], _i),
+        "vg_filter_pointcloud_device": ([_p, _sz, _f, _f, _p, _p, _p, _i, _p, _p, _p], _i),
+        "vg_filter_pointcloud": ([_p, _sz, _f, _f, _p, _p, _p, _i, _p, _p, _p], _i),
         "vg_env_pointcloud_layout": ([_p, _i, _p, _p, _p, _p, _p, _p], _i),
         "vg_env_set_mode": ([_p, _i, _i], _i),
         "vg_env_set_schedule": ([_p, _i], _i),
@@ -110,6 +112,8 @@ EXPORTED = (
     "vg_env_add_cuboid",
     "vg_env_add_pointcloud",
     "vg_env_add_pointcloud_device",
+    "vg_filter_pointcloud_device",
+    "vg_filter_pointcloud",
     "vg_env_pointcloud_layout",
     "vg_env_set_mode",
     "vg_env_set_schedule",

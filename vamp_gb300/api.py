@@ -110,9 +110,9 @@ class Environment:
         is bit-identical to add_pointcloud's."""
         import torch
 
-        pts = points.detach().to(torch.float32).reshape(-1, 3).contiguous()
-        if not pts.is_cuda:
+        if not (isinstance(points, torch.Tensor) and points.is_cuda):
             raise ValueError("add_pointcloud_device takes a CUDA tensor")
+        pts = points.detach().to(torch.float32).reshape(-1, 3).contiguous()
         with torch.cuda.device(pts.device):
             check(lib.vg_env_add_pointcloud_device(self._h, pts.data_ptr(), pts.shape[0], float(r_min), float(r_max),
                                                    float(r_point), _stream(pts)))
@@ -317,6 +317,39 @@ def _stream(t):
     import torch
 
     return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def filter_pointcloud(pc, min_dist: float, max_range: float, origin, workcell_min, workcell_max, cull: bool):
+    """The reference's filter_pointcloud (collision/filter.hh:176-320; binding
+    bindings/environment.cc:167-197), run on the GPU: returns (kept points [m, 3] float32, elapsed
+    nanoseconds).  pc is an [n, 3] array or list of points in host memory."""
+    pts = np.ascontiguousarray(pc, np.float32).reshape(-1, 3)
+    out = np.zeros_like(pts)
+    o, lo, hi = (np.ascontiguousarray(v, np.float32).reshape(3) for v in (origin, workcell_min, workcell_max))
+    m = ctypes.c_size_t()
+    ns = ctypes.c_uint64()
+    check(lib.vg_filter_pointcloud(_ptr(pts), len(pts), float(min_dist), float(max_range), _ptr(o), _ptr(lo), _ptr(hi),
+                                   int(bool(cull)), _ptr(out), ctypes.byref(m), ctypes.byref(ns)))
+    return out[: m.value].copy(), ns.value
+
+
+def filter_pointcloud_device(points, min_dist: float, max_range: float, origin, workcell_min, workcell_max,
+                             cull: bool):
+    """filter_pointcloud on a CUDA tensor of points [n, 3] (float32): the kept points as a CUDA
+    tensor [m, 3], on the current stream."""
+    import torch
+
+    if not (isinstance(points, torch.Tensor) and points.is_cuda):
+        raise ValueError("filter_pointcloud_device takes a CUDA tensor")
+    pts = points.detach().to(torch.float32).reshape(-1, 3).contiguous()
+    out = torch.empty_like(pts)
+    o, lo, hi = (np.ascontiguousarray(v, np.float32).reshape(3) for v in (origin, workcell_min, workcell_max))
+    m = ctypes.c_size_t()
+    with torch.cuda.device(pts.device):
+        check(lib.vg_filter_pointcloud_device(pts.data_ptr(), pts.shape[0], float(min_dist), float(max_range), _ptr(o),
+                                              _ptr(lo), _ptr(hi), int(bool(cull)), out.data_ptr(), ctypes.byref(m),
+                                              _stream(pts)))
+    return out[: m.value]
 
 
 def autotune(robot: Robot, environment: Environment, starts, goals, resolution: int | None = None) -> dict:
