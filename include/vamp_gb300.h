@@ -103,6 +103,20 @@ int vg_filter_pointcloud(const float *xyz, size_t n, float min_dist, float max_r
  * sizes. */
 int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, float *tests, float *aabbs,
                              uint32_t *aff_starts, float *aff, float *top);
+/* An attachment (collision/attachments.hh:11-56; Environment.attach / detach,
+ * bindings/environment.cc:162-165; vamp.Attachment, :200-230): k spheres {x, y, z, r} in a frame
+ * at the row-major 4x4 transform tf16 from the robot's end effector.  The environment copies
+ * them; while attached, every check runs Robot::fkcc_attach (robots/panda.hh:10265-15445, chosen
+ * by planning/validate.hh:43,58), which also tests the posed spheres against the environment and
+ * the robot links the reference lists.  At most VG_MAX_ATTACH_SPHERES spheres. */
+#define VG_MAX_ATTACH_SPHERES 64
+int vg_env_attach(vg_env *env, const float *tf16, const float *spheres, size_t k);
+int vg_env_detach(vg_env *env);
+/* Robot::eefk (robots/panda.hh:15447-15552; binding robot_helper.hh:302-305,580): the end
+ * effector's transform, row-major 4x4, for configurations q[n][dim].  _device: q and out on the
+ * current GPU (stream-ordered); host form: host buffers (synchronous). */
+int vg_eefk_device(const char *robot, const float *q, size_t n, float *out, void *stream);
+int vg_eefk(const char *robot, const float *q, size_t n, float *out);
 /* Which reference build to reproduce: lanes 8 + VG_SQRT_X86 (default) or lanes 4 + VG_SQRT_EXACT. */
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
 /* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):

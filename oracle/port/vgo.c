@@ -61,13 +61,34 @@ struct vgo_env
     vgo_capt *clouds[VGO_MAX_CLOUDS];
     int n_clouds;
     int sqrt_mode;
+    /* attachment: relative transform rows {R[r][0], R[r][1], R[r][2], t[r]}, then spheres */
+    int n_att; /* -1: none attached */
+    float att[12 + 4 * VGO_MAX_ATTACH];
 };
 
 vgo_env *vgo_env_create(void)
 {
     vgo_env *e = (vgo_env *)calloc(1, sizeof(vgo_env));
     e->sqrt_mode = VGO_SQRT_X86;
+    e->n_att = -1;
     return e;
+}
+
+int vgo_env_attach(vgo_env *e, const float *tf16, const float *spheres, int k)
+{
+    if (k < 0 || k > VGO_MAX_ATTACH)
+        return -1;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c)
+            e->att[4 * r + c] = tf16[4 * r + c];
+    memcpy(e->att + 12, spheres, (size_t)k * 4 * sizeof(float));
+    e->n_att = k;
+    return 0;
+}
+
+void vgo_env_detach(vgo_env *e)
+{
+    e->n_att = -1;
 }
 
 void vgo_env_destroy(vgo_env *e)
@@ -338,6 +359,7 @@ const struct vgo_capt *vgo_env_capt(const vgo_env *e, int idx)
 
 typedef void (*spheres32_fn)(const float *, float *);
 typedef void (*spheres64_fn)(const double *, double *);
+typedef void (*pose32_fn)(const float *, float *);
 
 struct vgo_robot
 {
@@ -350,6 +372,9 @@ struct vgo_robot
     const int *env_coarse, *env_start, *env_fine;
     int n_self;
     const int *self_coarse, *self_start, *self_fine;
+    pose32_fn ee_pose;
+    int n_attach;
+    const int *attach_coarse, *attach_start, *attach_fine;
 };
 
 #define VGO_ROBOT(nm, NM)                                                                                   \
@@ -357,7 +382,9 @@ struct vgo_robot
         #nm, VGO_##NM##_DIM, VGO_##NM##_FINE, VGO_##NM##_SLOTS, VGO_##NM##_RESOLUTION, vgo_##nm##_s_m,     \
             vgo_##nm##_s_a, vgo_##nm##_spheres_f32, vgo_##nm##_spheres_f64, VGO_##NM##_ENV_CHECKS,         \
             vgo_##nm##_env_coarse, vgo_##nm##_env_start, vgo_##nm##_env_fine, VGO_##NM##_SELF_CHECKS,      \
-            vgo_##nm##_self_coarse, vgo_##nm##_self_start, vgo_##nm##_self_fine                            \
+            vgo_##nm##_self_coarse, vgo_##nm##_self_start, vgo_##nm##_self_fine, vgo_##nm##_ee_pose_f32,   \
+            VGO_##NM##_ATTACH_LINKS, vgo_##nm##_attach_coarse, vgo_##nm##_attach_start,                    \
+            vgo_##nm##_attach_fine                                                                         \
     }
 
 static const struct vgo_robot kRobots[] = {
@@ -412,6 +439,7 @@ void vgo_robot_limits(const vgo_robot *r, float *s_m, float *s_a)
 }
 
 void vgo_robot_spheres_f32(const vgo_robot *r, const float *q, float *out) { r->f32(q, out); }
+void vgo_robot_ee_pose(const vgo_robot *r, const float *q, float *T) { r->ee_pose(q, T); }
 void vgo_robot_spheres_f64(const vgo_robot *r, const double *q, double *out) { r->f64(q, out); }
 
 /* sphere_sphere_self_collision (validity.hh:23-44) for one block: any lane negative */
@@ -443,9 +471,91 @@ static int env_block(const vgo_env *e, int lanes, const float *S, int slot)
     return vgo_sphere_env(e, lanes, x, y, z, r);
 }
 
+/* The attachment posed at the end effector (Attachment::pose, attachments.hh:43-55): the
+ * transform p_tf * tf, R = Rp Rt and t = Rp tt + tp, then each sphere centre R s + t.  Every
+ * entry is a chain of fused multiply-adds, first term first (the kernels use the same order). */
+static void att_pose(const float *T, const float *A, float *NR, float *Nt)
+{
+    for (int r = 0; r < 3; ++r)
+    {
+        for (int c = 0; c < 3; ++c)
+            NR[3 * r + c] = fmaf(T[3 * r + 2], A[8 + c], fmaf(T[3 * r + 1], A[4 + c], T[3 * r] * A[c]));
+        Nt[r] = fmaf(T[3 * r + 2], A[11], fmaf(T[3 * r + 1], A[7], fmaf(T[3 * r], A[3], T[9 + r])));
+    }
+}
+
+static void att_centre(const float *NR, const float *Nt, const float *s, float *c)
+{
+    for (int r = 0; r < 3; ++r)
+        c[r] = fmaf(NR[3 * r + 2], s[2], fmaf(NR[3 * r + 1], s[1], fmaf(NR[3 * r], s[0], Nt[r])));
+}
+
+/* attachment_sphere_collision (validity.hh:270-293) of one robot sphere slot per lane: any lane's
+ * sphere against any posed attachment sphere (sphere_sphere_sql2, robot sphere first) */
+static int att_robot_block(const vgo_env *e, int lanes, const float *S, const float *P, int slot)
+{
+    int hit = 0;
+    for (int k = 0; k < e->n_att; ++k)
+    {
+        const float ar = e->att[12 + 4 * k + 3];
+        for (int l = 0; l < lanes; ++l)
+        {
+            const float *a = S + (size_t)l * VGO_MAX_SLOTS * 4 + 4 * slot;
+            const float *b = P + ((size_t)l * VGO_MAX_ATTACH + k) * 3;
+            const float rs = a[3] + ar;
+            hit |= vgo_signbit(fmaf(-rs, rs, sql2(a[0], a[1], a[2], b[0], b[1], b[2])));
+        }
+        if (hit)
+            return 1;
+    }
+    return 0;
+}
+
+/* The attachment part of Robot::fkcc_attach (robots/panda.hh:15308-15445): the posed spheres
+ * against the environment (attachment_environment_collision, validity.hh:251-268), then per listed
+ * robot link its coarse sphere gating its fine spheres against the posed spheres.  Returns 1 if
+ * the block collides. */
+static int attach_block(const vgo_robot *r, const vgo_env *e, int lanes, const float *q, const float *S)
+{
+    static __thread float P[VGO_MAX_LANES * VGO_MAX_ATTACH * 3];
+    for (int l = 0; l < lanes; ++l)
+    {
+        float T[12], NR[9], Nt[3];
+        r->ee_pose(q + (size_t)l * r->dim, T);
+        att_pose(T, e->att, NR, Nt);
+        for (int k = 0; k < e->n_att; ++k)
+            att_centre(NR, Nt, e->att + 12 + 4 * k, P + ((size_t)l * VGO_MAX_ATTACH + k) * 3);
+    }
+    for (int k = 0; k < e->n_att; ++k)
+    {
+        float x[VGO_MAX_LANES], y[VGO_MAX_LANES], z[VGO_MAX_LANES], rad[VGO_MAX_LANES];
+        for (int l = 0; l < lanes; ++l)
+        {
+            const float *c = P + ((size_t)l * VGO_MAX_ATTACH + k) * 3;
+            x[l] = c[0];
+            y[l] = c[1];
+            z[l] = c[2];
+            rad[l] = e->att[12 + 4 * k + 3];
+        }
+        if (vgo_sphere_env(e, lanes, x, y, z, rad))
+            return 1;
+    }
+    for (int c = 0; c < r->n_attach; ++c)
+    {
+        if (!att_robot_block(e, lanes, S, P, r->attach_coarse[c]))
+            continue;
+        for (int k = r->attach_start[c]; k < r->attach_start[c + 1]; ++k)
+            if (att_robot_block(e, lanes, S, P, r->attach_fine[k]))
+                return 1;
+    }
+    return 0;
+}
+
 /* Robot::fkcc (robots/panda.hh:5227-10262): FK of every sphere, then environment checks link by
  * link (coarse sphere gating fine spheres), then self-collision link pairs (coarse pair gating
- * fine pairs).  Any failing fine test invalidates the whole block. */
+ * fine pairs).  Any failing fine test invalidates the whole block.  With an attachment in the
+ * environment, Robot::fkcc_attach (panda.hh:10265-15445, chosen by validate.hh:43,58): the same,
+ * then the attachment checks. */
 int vgo_fkcc(const vgo_robot *r, const vgo_env *e, int lanes, const float *q)
 {
     static __thread float S[VGO_MAX_LANES * VGO_MAX_SLOTS * 4];
@@ -469,6 +579,8 @@ int vgo_fkcc(const vgo_robot *r, const vgo_env *e, int lanes, const float *q)
             if (self_block(lanes, S, r->self_fine[2 * k], r->self_fine[2 * k + 1]))
                 return 0;
     }
+    if (e->n_att >= 0 && attach_block(r, e, lanes, q, S))
+        return 0;
     return 1;
 }
 

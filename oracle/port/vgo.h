@@ -35,6 +35,14 @@ void vgo_env_add_cuboid(vgo_env *e, const float *f);
 /* pointcloud as a CAPT (capt.hh:294-365); returns 0 on success */
 int vgo_env_add_pointcloud(vgo_env *e, const float *xyz, size_t n, float r_min, float r_max, float r_point);
 void vgo_env_set_sqrt_mode(vgo_env *e, int mode); /* VGO_SQRT_X86 (default) or VGO_SQRT_EXACT */
+/* Attachment (collision/attachments.hh; bindings/environment.cc:163-165,200-230): spheres [k][4]
+ * in a frame at the relative transform tf (4x4, row-major) from the end effector; checked by
+ * fkcc_attach.  Returns 0 on success (k <= VGO_MAX_ATTACH). */
+#define VGO_MAX_ATTACH 64
+int vgo_env_attach(vgo_env *e, const float *tf16, const float *spheres, int k);
+void vgo_env_detach(vgo_env *e);
+/* end-effector transform of one configuration: R row-major (9), then t (3) (Robot::eefk) */
+void vgo_robot_ee_pose(const vgo_robot *r, const float *q, float *T);
 /* kind 0..4: spheres, capsules, z-capsules, cuboids, z-cuboids; sorted by min_distance */
 size_t vgo_env_count(const vgo_env *e, int kind);
 /* fields of the idx-th object of a kind followed by its min_distance; returns the float count */

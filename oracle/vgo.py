@@ -140,6 +140,9 @@ class Port:
         lib.vgo_env_total.argtypes = [_p]
         lib.vgo_robot_self_pairs.argtypes = [_p]
         lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
+        lib.vgo_env_attach.argtypes = [_p, _p, _p, ctypes.c_int]
+        lib.vgo_env_detach.argtypes = [_p]
+        lib.vgo_robot_ee_pose.argtypes = [_p, _p, _p]
         lib.vgo_filter_pointcloud.argtypes = [_p, _sz, _f, _f, _p, _p, _p, ctypes.c_int, _p]
         lib.vgo_filter_pointcloud.restype = _sz
         lib.vgo_filter_remap.argtypes = [_f, _f, _f]
@@ -209,6 +212,16 @@ class PortRobot:
         self.port.lib.vgo_robot_spheres_f32(self.h, _ptr(q), _ptr(out))
         return out
 
+    def ee_pose(self, q: np.ndarray) -> np.ndarray:
+        """End-effector transform as a row-major 4x4 (R row-major and t, as the kernels compute it)."""
+        q = np.ascontiguousarray(q, np.float32)
+        T = np.zeros(12, np.float32)
+        self.port.lib.vgo_robot_ee_pose(self.h, _ptr(q), _ptr(T))
+        out = np.eye(4, dtype=np.float32)
+        out[:3, :3] = T[:9].reshape(3, 3)
+        out[:3, 3] = T[9:]
+        return out
+
     def spheres_f64(self, q: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(q, np.float64)
         out = np.zeros((self.slots, 4), np.float64)
@@ -233,6 +246,11 @@ class PortEnv:
             rc = lib.vgo_env_add_pointcloud(self.h, _ptr(pts), len(pts), pc["r_min"], pc["r_max"], pc["r_point"])
             if rc:
                 raise RuntimeError("pointcloud rejected")
+        if scene.get("attachment") is not None:
+            tf = np.ascontiguousarray(scene["attachment"]["tf"], np.float32).reshape(16)
+            sph = np.ascontiguousarray(scene["attachment"]["spheres"], np.float32).reshape(-1, 4)
+            if lib.vgo_env_attach(self.h, _ptr(tf), _ptr(sph), len(sph)):
+                raise RuntimeError("attachment rejected")
 
     def __del__(self):
         try:

@@ -67,17 +67,39 @@ def filter_fixtures(ref: Reference) -> None:
     np.savez_compressed(OUT / "filter.npz", **out)
 
 
+def eefk_fixtures(reference: Path) -> None:
+    """Robot::eefk (robots/<robot>.hh): the reference's own end-effector expressions evaluated in
+    float64 on sampled configurations, as row-major 4x4 transforms."""
+    from vamp_gb300.robotgen.extract import eefk_statements, evaluate
+
+    for r in ROBOTS:
+        text = (reference / "src/impl/vamp/robots" / f"{r}.hh").read_text()
+        stmts = eefk_statements(text)
+        rb = Port().robot(r)
+        q = scenes.configurations(rb.s_m, rb.s_a, 64, 300 + len(r))
+        T = np.zeros((len(q), 4, 4))
+        for i, qi in enumerate(q):
+            y = evaluate(stmts, qi.astype(np.float64))
+            T[i, :3, 3] = [y[0], y[1], y[2]]
+            T[i, :3, :3] = np.array([y[3 + k] for k in range(9)]).reshape(3, 3).T  # column-major
+            T[i, 3, 3] = 1.0
+        np.savez_compressed(OUT / f"eefk_{r}.npz", q=q, T=T)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None)
-    ap.add_argument("--only", choices=["filter"], default=None, help="regenerate one group of fixtures")
+    ap.add_argument("--only", choices=["filter", "eefk"], default=None, help="regenerate one group of fixtures")
     a = ap.parse_args()
     if build_reference(a.reference) is None:
         raise SystemExit("reference checkout not found (or not x86-64): cannot generate golden fixtures")
     ref = Reference()
     port = Port()
-    filter_fixtures(ref)
-    if a.only == "filter":
+    if a.only in (None, "filter"):
+        filter_fixtures(ref)
+    if a.only in (None, "eefk"):
+        eefk_fixtures(Path(a.reference or "/root/reference"))
+    if a.only is not None:
         return
 
     # --- forward kinematics: fine sphere centres (Robot::sphere_fk)

@@ -184,3 +184,42 @@ def test_filter_conversion_and_morton(port):
     assert lib.vgo_morton(1, 0, 0) == 1 and lib.vgo_morton(0, 1, 0) == 2 and lib.vgo_morton(0, 0, 1) == 4
     assert lib.vgo_morton(0x7FF, 0, 0) == 0x49249249 and lib.vgo_morton(0, 0x7FF, 0) == 0x92492492
     assert lib.vgo_morton(0, 0, 0x7FF) == 0x24924924  # z keeps 10 bits
+
+
+@pytest.mark.parametrize("robot", ["panda", "ur5", "fetch", "baxter"])
+def test_ee_pose_matches_the_reference_eefk(port, robot):
+    """The end-effector transform the attachment is posed at, against the reference's own eefk
+    expressions (robots/<robot>.hh, Robot::eefk) evaluated in float64: FP32 rounding only."""
+    g = golden(f"eefk_{robot}")
+    rb = port.robot(robot)
+    err = max(np.abs(rb.ee_pose(q) - T).max() for q, T in zip(g["q"], g["T"]))
+    assert err < 1e-5, err
+
+
+def _attach_scene(scene: dict, spheres, offset: float = 0.14) -> dict:
+    tf = np.eye(4, dtype=np.float32)
+    tf[2, 3] = offset
+    return {**scene, "attachment": {"tf": tf, "spheres": np.asarray(spheres, np.float32).reshape(-1, 4)}}
+
+
+def test_attachment_checks_in_the_oracle(port):
+    """fkcc_attach in the oracle: an attachment far from everything changes no verdict; one that
+    engulfs the workspace fails every configuration; a sphere at the hand only adds failures."""
+    from vamp_gb300 import scenes
+
+    rb = port.robot("panda")
+    base = scenes.scene_config1(5)
+    q = scenes.configurations(rb.s_m, rb.s_a, 600, 9)
+    plain = port.env(base).validate_states(rb, q)
+    far = port.env(_attach_scene(base, [[0, 0, 0, 0.001]], offset=50.0)).validate_states(rb, q)
+    assert np.array_equal(plain, far)
+    huge = port.env(_attach_scene(base, [[0, 0, 0, 3.0]])).validate_states(rb, q)
+    assert not huge.any()
+    hand = port.env(_attach_scene(base, [[0, 0, 0, 0.07]])).validate_states(rb, q)
+    assert not (hand & ~plain).any() and (plain & ~hand).any()
+    # the attachment against the robot itself: empty scene, a large sphere near the hand
+    empty = {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+             "cuboids": np.zeros((0, 15), np.float32)}
+    self_only = port.env(_attach_scene(empty, [[0, 0, 0, 0.25]], offset=0.0)).validate_states(rb, q)
+    plain_empty = port.env(empty).validate_states(rb, q)
+    assert (plain_empty & ~self_only).any()

@@ -15,7 +15,8 @@ access raises ImportError (there is no CPU fallback).  Submodules that do not ne
 from __future__ import annotations
 
 _API = {"Environment", "Robot", "VampError", "SQRT_X86", "SQRT_EXACT", "panda", "ur5", "fetch", "baxter", "ROBOTS",
-        "autotune", "Batch", "CollisionPredictor", "SCHEDULES", "filter_pointcloud", "filter_pointcloud_device"}
+        "autotune", "Batch", "CollisionPredictor", "SCHEDULES", "filter_pointcloud", "filter_pointcloud_device",
+        "Attachment"}
 
 
 def __getattr__(name):

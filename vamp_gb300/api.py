@@ -98,6 +98,10 @@ class Environment:
             env.add_cuboid(c)
         for pc in scene.get("pointclouds", []):
             env.add_pointcloud(pc["points"], pc["r_min"], pc["r_max"], pc["r_point"])
+        if scene.get("attachment") is not None:
+            a = Attachment(scene["attachment"]["tf"])
+            a.add_spheres(np.asarray(scene["attachment"]["spheres"], np.float32).reshape(-1, 4))
+            env.attach(a)
         return env
 
     def add_pointcloud(self, points, r_min: float, r_max: float, r_point: float) -> None:
@@ -116,6 +120,16 @@ class Environment:
         with torch.cuda.device(pts.device):
             check(lib.vg_env_add_pointcloud_device(self._h, pts.data_ptr(), pts.shape[0], float(r_min), float(r_max),
                                                    float(r_point), _stream(pts)))
+
+    def attach(self, attachment: "Attachment") -> None:
+        """Attach spheres to the end effector (Environment.attach, bindings/environment.cc:162-164):
+        a copy of the attachment; every later check runs fkcc_attach."""
+        tf = np.ascontiguousarray(attachment.relative_frame, np.float32).reshape(16)
+        sph = np.ascontiguousarray(attachment.spheres, np.float32).reshape(-1, 4)
+        check(lib.vg_env_attach(self._h, _ptr(tf), _ptr(sph), len(sph)))
+
+    def detach(self) -> None:
+        check(lib.vg_env_detach(self._h))
 
     def pointcloud_layout(self, index: int = 0) -> dict:
         sizes = np.zeros(4, np.uint64)
@@ -207,6 +221,14 @@ class Robot:
         if check_bounds and not (self._in_bounds(a[0]) and self._in_bounds(b[0])):
             return False
         return bool(self.validate_motion_batch(a, b, environment, resolution)[0])
+
+    def eefk(self, configuration) -> np.ndarray:
+        """End-effector transform, a row-major 4x4 float32 matrix (Robot::eefk; binding
+        robot_helper.hh:302-305)."""
+        q = np.ascontiguousarray(configuration, np.float32).reshape(-1, self._dim)
+        out = np.zeros((len(q), 4, 4), np.float32)
+        check(lib.vg_eefk(self._b, _ptr(q), len(q), _ptr(out)))
+        return out[0] if np.ndim(configuration) == 1 else out
 
     def fk(self, configuration) -> np.ndarray:
         """Fine sphere centres and radii [n_spheres, 4] (Robot::sphere_fk)."""
@@ -317,6 +339,31 @@ def _stream(t):
     import torch
 
     return torch.cuda.current_stream(t.device).cuda_stream
+
+
+class Attachment:
+    """Spheres carried by the end effector (collision/attachments.hh:11-56; the binding
+    vamp.Attachment, bindings/environment.cc:200-230): a relative frame (4x4 transform from the
+    end effector) and spheres [x, y, z, r] in that frame.  Environment.attach copies it."""
+
+    def __init__(self, tf):
+        self.relative_frame = np.array(tf, np.float32).reshape(4, 4)
+        self.spheres = np.zeros((0, 4), np.float32)
+        self.posed_spheres = np.zeros((0, 4), np.float32)
+
+    def add_sphere(self, sphere) -> None:
+        self.add_spheres([sphere])
+
+    def add_spheres(self, spheres) -> None:
+        rows = [np.asarray(_fields(s, ("x", "y", "z", "r")), np.float32).reshape(4) for s in spheres]
+        self.spheres = np.concatenate([self.spheres, np.array(rows, np.float32).reshape(-1, 4)])
+
+    def set_ee_pose(self, tf) -> None:
+        """posed_spheres at the end-effector transform tf (Attachment::pose; for display: the
+        checks pose the spheres on the GPU)."""
+        T = np.asarray(tf, np.float64).reshape(4, 4) @ self.relative_frame.astype(np.float64)
+        c = self.spheres[:, :3].astype(np.float64) @ T[:3, :3].T + T[:3, 3]
+        self.posed_spheres = np.concatenate([c, self.spheres[:, 3:4]], axis=1).astype(np.float32)
 
 
 def filter_pointcloud(pc, min_dist: float, max_range: float, origin, workcell_min, workcell_max, cull: bool):

@@ -240,6 +240,13 @@ namespace vg
         std::vector<float4> img;
         pack_image(e, img, e->off, e->n);
         pack_clouds(e, img, &e->cloud_off);
+        // the attachment: 3 transform rows, then its spheres
+        e->att_off = static_cast<int>(img.size());
+        if (e->n_att >= 0)
+        {
+            for (int k = 0; k < 3 + e->n_att; ++k)
+                img.push_back(make_float4(e->att[4 * k], e->att[4 * k + 1], e->att[4 * k + 2], e->att[4 * k + 3]));
+        }
         if (img.size() > e->image_cap)
         {
             if (e->d_image)
@@ -275,6 +282,8 @@ namespace vg
         d.sqrt_mode = e->sqrt_mode;
         d.n_clouds = static_cast<int>(e->clouds.size());
         d.cloud_off = e->cloud_off;
+        d.n_att = e->n_att;
+        d.att_off = e->att_off;
         return d;
     }
 
@@ -347,11 +356,15 @@ namespace vg
         const vg_env *env = m.env;
         const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
         const int which = env->lanes == 8 ? 0 : 1;
-        const bool learned = m.scores != nullptr;
-        const bool grouped = learned || m.schedule >= 1;
-        const bool wide = !learned && m.schedule == 2;
-        const void *fn = learned ? r->edges_learned_fn[which]
-                                 : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
+        // with an attachment every schedule runs fkcc_attach in the segment-per-edge kernel (the
+        // block order does not change verdicts, so a learned order is not needed there)
+        const bool attach = env->n_att >= 0;
+        const bool learned = !attach && m.scores != nullptr;
+        const bool grouped = !attach && (learned || m.schedule >= 1);
+        const bool wide = grouped && !learned && m.schedule == 2;
+        const void *fn = attach ? r->edges_attach_fn[which]
+                                : learned ? r->edges_learned_fn[which]
+                                          : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
         int occ = 0;
         if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
             return rc;
@@ -364,8 +377,9 @@ namespace vg
         const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
         const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
         EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes};
-        const auto launch = learned ? r->edges_learned[which]
-                                    : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
+        const auto launch = attach ? r->edges_attach[which]
+                                   : learned ? r->edges_learned[which]
+                                             : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
         VG_CUDA(launch(p, grid, kBlock, smem, s), "edges kernel launch");
         return VG_OK;
     }
@@ -671,13 +685,68 @@ int vg_validate_states_device(const char *robot, vg_env *env, const float *q, si
     if (int rc = commit(env))
         return rc;
     const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
+    const bool attach = env->n_att >= 0;
     int occ = 0;
-    if (int rc = prepare_kernel(r->states_fn, smem, kBlock, &occ))
+    if (int rc = prepare_kernel(attach ? r->states_attach_fn : r->states_fn, smem, kBlock, &occ))
         return rc;
     const long long want = (static_cast<long long>(n) + kBlock - 1) / kBlock;
     const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
     StatesParams p{q, static_cast<long long>(n), out, env_device(env)};
-    VG_CUDA(r->states(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)), "states kernel launch");
+    VG_CUDA((attach ? r->states_attach : r->states)(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)),
+            "states kernel launch");
+    return VG_OK;
+}
+
+int vg_env_attach(vg_env *env, const float *tf16, const float *spheres, size_t k)
+{
+    if (!env || !tf16 || (k && !spheres))
+        return set_error(VG_ERR_ARG, "vg_env_attach: null argument");
+    if (k > static_cast<size_t>(VG_MAX_ATTACH_SPHERES))
+        return set_error(VG_ERR_LIMIT, "vg_env_attach: at most 64 spheres per attachment");
+    env->att.assign(tf16, tf16 + 12);  // rows 0..2 of the row-major 4x4 transform
+    env->att.insert(env->att.end(), spheres, spheres + 4 * k);
+    env->n_att = static_cast<int>(k);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_detach(vg_env *env)
+{
+    if (!env)
+        return set_error(VG_ERR_ARG, "vg_env_detach: null argument");
+    env->att.clear();
+    env->n_att = -1;
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_eefk_device(const char *robot, const float *q, size_t n, float *out, void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_eefk_device: bad argument");
+    VG_CUDA(r->ee_pose(q, static_cast<long long>(n), out, static_cast<cudaStream_t>(stream)), "eefk kernel launch");
+    return VG_OK;
+}
+
+int vg_eefk(const char *robot, const float *q, size_t n, float *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || (n && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_eefk: bad argument");
+    if (n == 0)
+        return VG_OK;
+    float *d = nullptr;
+    const size_t in_bytes = n * r->dim * sizeof(float), out_bytes = n * 16 * sizeof(float);
+    VG_CUDA(cudaMalloc(&d, in_bytes + out_bytes), "vg_eefk: cudaMalloc");
+    cudaError_t e = cudaMemcpy(d, q, in_bytes, cudaMemcpyHostToDevice);
+    float *d_out = d + n * r->dim;
+    if (e == cudaSuccess)
+        e = r->ee_pose(d, static_cast<long long>(n), d_out, nullptr);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, d_out, out_bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    VG_CUDA(e, "vg_eefk");
     return VG_OK;
 }
 

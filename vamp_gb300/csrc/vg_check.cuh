@@ -191,6 +191,8 @@ namespace vg
         int sqrt_mode;
         const CaptView *clouds;
         int n_clouds;
+        const float4 *att;  // attachment: 3 transform rows {R[r][0..2], t[r]}, then spheres
+        int n_att;          // -1: none
     };
 
     __device__ __forceinline__ float sql2(float ax, float ay, float az, float bx, float by, float bz)

@@ -34,6 +34,13 @@ namespace vg
         // same-edge schedule in a learned block order (EdgesParams::scores)
         cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_learned_fn[2];
+        // fkcc_attach forms (an attachment in the environment): states, and edges a segment each
+        cudaError_t (*states_attach)(const StatesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *states_attach_fn;
+        cudaError_t (*edges_attach[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_attach_fn[2];
+        // Robot::eefk: row-major 4x4 transforms [n][16] from configurations [n][dim]
+        cudaError_t (*ee_pose)(const float *, long long, float *, cudaStream_t);
         int stage_floats;  // shared-memory staging floats per thread (after the environment image)
         cudaError_t (*spheres)(const float *, long long, float *, cudaStream_t);
         // fkcc_debug's self part: flags [n][self_pairs] from sphere slots [n][slots][4]
@@ -89,6 +96,11 @@ struct vg_env
     size_t image_f4 = 0, image_cap = 0;
     int off[5] = {0, 0, 0, 0, 0};
     int cloud_off = 0;
+    // attachment (vg_env_attach): relative transform rows {R[r][0..2], t[r]}, then spheres
+    // {x, y, z, r}; n_att = -1 while none is attached
+    int n_att = -1;
+    std::vector<float> att;
+    int att_off = 0;
     int n[5] = {0, 0, 0, 0, 0};
     // pointclouds: host trees and their device copies (tests, aabbs, starts, aff per cloud)
     std::vector<vg::CaptHost> clouds;

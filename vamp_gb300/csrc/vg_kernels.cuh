@@ -42,6 +42,8 @@ namespace vg
         int sqrt_mode;
         int n_clouds;       // CaptView descriptors at the end of the image
         int cloud_off;      // their offset, in float4
+        int n_att;          // attachment spheres (-1: no attachment)
+        int att_off;        // attachment block: 3 transform rows, then the spheres, in float4
     };
 
     constexpr int kRsqrtF4 = 2048 / 4;
@@ -67,6 +69,8 @@ namespace vg
         v.sqrt_mode = d.sqrt_mode;
         v.clouds = reinterpret_cast<const CaptView *>(smem + d.cloud_off - kRsqrtF4);
         v.n_clouds = d.n_clouds;
+        v.att = smem + d.att_off - kRsqrtF4;
+        v.n_att = d.n_att;
         for (int k = 0; k < 5; ++k)
         {
             v.rec[k] = smem + d.off[k] - kRsqrtF4;
@@ -75,14 +79,94 @@ namespace vg
         return v;
     }
 
-    // kLoopedEnv: the robot's environment section as loops (smaller code) instead of unrolled
-    template <typename Robot, int W, bool kLoopedEnv = false>
+    // The attachment part of Robot::fkcc_attach (robots/panda.hh:15308-15445) for the segments
+    // in `alive`: the attachment's spheres posed at the end effector (Attachment::pose,
+    // collision/attachments.hh:43-55: p_tf * tf, then each centre) against the environment
+    // (attachment_environment_collision, validity.hh:251-268), then, per robot link the
+    // reference lists, its coarse sphere gating its fine spheres against the posed spheres
+    // (attachment_sphere_collision, validity.hh:270-293).  Returns the segments still valid.
+    // Every product is a chain of fused multiply-adds, first term first.
+    template <typename Robot, int W>
+    __device__ __noinline__ unsigned attach_check(const EnvView &ev, const float *q, unsigned alive)
+    {
+        CheckCtx<W> ctx{ev, alive, false, nullptr, nullptr};
+        float T[12], NR[9], Nt[3];
+        Robot::ee_pose(q, T);
+        const float4 *A = ev.att;
+        const float a[3][4] = {{A[0].x, A[0].y, A[0].z, A[0].w}, {A[1].x, A[1].y, A[1].z, A[1].w},
+                               {A[2].x, A[2].y, A[2].z, A[2].w}};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                NR[3 * r + c] = __fmaf_rn(T[3 * r + 2], a[2][c], __fmaf_rn(T[3 * r + 1], a[1][c], __fmul_rn(T[3 * r], a[0][c])));
+            Nt[r] = __fmaf_rn(T[3 * r + 2], a[2][3], __fmaf_rn(T[3 * r + 1], a[1][3], __fmaf_rn(T[3 * r], a[0][3], T[9 + r])));
+        }
+        auto posed = [&](int k) {
+            const float4 s = A[3 + k];
+            float c[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                c[r] = __fmaf_rn(NR[3 * r + 2], s.z, __fmaf_rn(NR[3 * r + 1], s.y, __fmaf_rn(NR[3 * r], s.x, Nt[r])));
+            return make_float4(c[0], c[1], c[2], s.w);
+        };
+        unsigned need = ctx.alive;
+#pragma unroll 1
+        for (int k = 0; k < ev.n_att && need; ++k)
+        {
+            const float4 c = posed(k);
+            const unsigned hit = ctx.env_hit(c.x, c.y, c.z, c.w, need);
+            ctx.alive &= ~hit;
+            need &= ~hit;
+        }
+        if (!need)
+            return ctx.alive;
+        float S[Robot::kSlots * 4];
+        Robot::spheres(q, S);
+        // any posed sphere against robot slot `slot`, for the segments in m
+        auto robot_hit = [&](int slot, unsigned m) {
+            unsigned hit = 0;
+#pragma unroll 1
+            for (int k = 0; k < ev.n_att && (m & ~hit); ++k)
+            {
+                const float4 c = posed(k);
+                hit |= ctx.self_hit(S[4 * slot], S[4 * slot + 1], S[4 * slot + 2], S[4 * slot + 3], c.x, c.y, c.z, c.w,
+                                    m & ~hit);
+            }
+            return hit;
+        };
+#pragma unroll 1
+        for (int L = 0; L < Robot::kAttachLinks && need; ++L)
+        {
+            const int4 li = Robot::attach_link(L);
+            unsigned gate = robot_hit(li.x, need);
+#pragma unroll 1
+            for (int f = li.y; f < li.z && gate; ++f)
+            {
+                const unsigned hit = robot_hit(Robot::attach_fine(f), gate);
+                ctx.alive &= ~hit;
+                need &= ~hit;
+                gate &= ~hit;
+            }
+        }
+        return ctx.alive;
+    }
+
+    // kLoopedEnv: the robot's environment section as loops (smaller code) instead of unrolled;
+    // kAttach: Robot::fkcc_attach (the environment holds an attachment)
+    template <typename Robot, int W, bool kLoopedEnv = false, bool kAttach = false>
     __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
         static_assert(Robot::kEnvChecks <= kWarpScratch, "per-warp scratch holds one word per environment check");
         __shared__ unsigned warp_scratch[kStageStride / 32][kWarpScratch];
         CheckCtx<W> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
         Robot::template fkcc<CheckCtx<W>, kLoopedEnv>(q, ctx);
+        if constexpr (kAttach)
+        {
+            if (ctx.alive)
+                ctx.alive = attach_check<Robot, W>(ev, q, ctx.alive);
+        }
         return ctx.alive;
     }
 
@@ -96,7 +180,7 @@ namespace vg
         EnvDevice env;
     };
 
-    template <typename Robot>
+    template <typename Robot, bool kAttach = false>
     __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) states_kernel(StatesParams p)
     {
         extern __shared__ float4 smem[];
@@ -117,7 +201,7 @@ namespace vg
             {
                 q[d] = in ? p.q[idx * D + d] : 0.0f;
             }
-            const unsigned alive = run_fkcc<Robot, 1, true>(ev, q, __ballot_sync(kFull, in), stage);
+            const unsigned alive = run_fkcc<Robot, 1, true, kAttach>(ev, q, __ballot_sync(kFull, in), stage);
             if (in)
             {
                 p.out[idx] = static_cast<uint8_t>((alive >> (threadIdx.x & 31)) & 1u);
@@ -237,7 +321,7 @@ namespace vg
         return __fsqrt_rn(__fadd_rn(__fadd_rn(a0, a2), __fadd_rn(a1, a3)));
     }
 
-    template <typename Robot, int W>
+    template <typename Robot, int W, bool kAttach = false>
     __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
@@ -307,7 +391,7 @@ namespace vg
             {
                 break;
             }
-            const unsigned alive = run_fkcc<Robot, W>(ev, q, active, stage);
+            const unsigned alive = run_fkcc<Robot, W, false, kAttach>(ev, q, active, stage);
             bool finish = false;
             if (e >= 0)
             {
@@ -654,5 +738,35 @@ namespace vg
             qq[d] = q[idx * Robot::kDim + d];
         }
         Robot::spheres(qq, out + idx * Robot::kSlots * 4);
+    }
+
+    // Robot::eefk (robots/panda.hh:15447-15552): the end effector's transform as a row-major 4x4
+    // matrix per configuration.
+    template <typename Robot>
+    __global__ void ee_pose_kernel(const float *q, long long n, float *out)
+    {
+        const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (idx >= n)
+        {
+            return;
+        }
+        float qq[Robot::kDim], T[12];
+        for (int d = 0; d < Robot::kDim; ++d)
+        {
+            qq[d] = q[idx * Robot::kDim + d];
+        }
+        Robot::ee_pose(qq, T);
+        float *o = out + idx * 16;
+        for (int r = 0; r < 3; ++r)
+        {
+            o[4 * r + 0] = T[3 * r + 0];
+            o[4 * r + 1] = T[3 * r + 1];
+            o[4 * r + 2] = T[3 * r + 2];
+            o[4 * r + 3] = T[9 + r];
+        }
+        o[12] = 0.0f;
+        o[13] = 0.0f;
+        o[14] = 0.0f;
+        o[15] = 1.0f;
     }
 }  // namespace vg

@@ -6,17 +6,28 @@
 
 namespace vg
 {
-    template <typename R>
+    template <typename R, bool kAttach = false>
     cudaError_t launch_states(const StatesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        states_kernel<R><<<grid, block, smem, s>>>(p);
+        states_kernel<R, kAttach><<<grid, block, smem, s>>>(p);
         return cudaGetLastError();
     }
 
-    template <typename R, int W>
+    template <typename R, int W, bool kAttach = false>
     cudaError_t launch_edges(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        edges_kernel<R, W><<<grid, block, smem, s>>>(p);
+        edges_kernel<R, W, kAttach><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
+    template <typename R>
+    cudaError_t launch_ee_pose(const float *q, long long n, float *out, cudaStream_t s)
+    {
+        if (n <= 0)
+        {
+            return cudaSuccess;
+        }
+        ee_pose_kernel<R><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(q, n, out);
         return cudaGetLastError();
     }
 
@@ -96,6 +107,14 @@ namespace vg
         o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
         o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);
         o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true>);
+        // fkcc_attach: the segment-per-edge and states kernels with the attachment checks
+        o.states_attach = &launch_states<R, true>;
+        o.states_attach_fn = reinterpret_cast<const void *>(&states_kernel<R, true>);
+        o.edges_attach[0] = &launch_edges<R, 8, true>;
+        o.edges_attach[1] = &launch_edges<R, 4, true>;
+        o.edges_attach_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8, true>);
+        o.edges_attach_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4, true>);
+        o.ee_pose = &launch_ee_pose<R>;
         o.stage_floats = R::kStage;
         o.spheres = &launch_spheres<R>;
         o.debug_self = &launch_debug_self<R>;

@@ -326,6 +326,27 @@ def emit_centre(em: Emitter, frames, kin: Kin, link: str, p, prefix: str):
     return out
 
 
+def emit_ee_pose(em: Emitter, frames, kin: Kin, link: str):
+    """Transform of `link` (the end effector, where fkcc_attach poses the attachment): its
+    frame's R and t composed with the constant link offset, R row-major then t, each entry one
+    lincomb (the same operation sequence as the frames themselves).  Returns 12 values."""
+    fid, C = kin.link_frame[link]
+    Rp, tp = frames[fid]
+    R = [[em.lincomb([(float(C[k, c]), Rp[r][k], None) for k in range(3)]) for c in range(3)] for r in range(3)]
+    t = [em.lincomb([(float(C[k, 3]), Rp[r][k], None) for k in range(3)] + [(1.0, tp[r], None)]) for r in range(3)]
+    return [R[r][c] for r in range(3) for c in range(3)] + t
+
+
+def attach_tables(model: dict, coarse_slot: dict):
+    """Per robot link checked against an attachment (fkcc_attach, in the reference's order): its
+    coarse slot and the range of its fine slots in the flat fine list."""
+    rows, fine = [], []
+    for c in model.get("attach_checks", []):
+        rows.append((coarse_slot[c["link"]], len(fine), len(fine) + len(c["fine"])))
+        fine += c["fine"]
+    return rows, fine
+
+
 # sin_ref + cos_ref of one joint angle: 24 + 25 floating-point operations (vg_check.cuh)
 SINCOS_FLOPS = 49
 # one sphere centre from its frame: 9 fused multiply-adds
@@ -625,6 +646,10 @@ def gen_cuda(model: dict) -> str:
         all_pairs = [tuple(p_) for e in model["self_checks"] for p_ in e["fine"]]
         w(f"    // every fine self pair, in the reference's order (debug reports; global memory)")
         w(f"    __device__ const int2 {pre}AllPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
+        arows, afine = attach_tables(model, coarse_slot)
+        w(f"    // links checked against an attachment (fkcc_attach): coarse slot, fine range; fine slots")
+        w(f"    __device__ const int4 {pre}AttachLink[{max(1, len(arows))}] = {{{', '.join('{%d, %d, %d, 0}' % r for r in arows) or '{0, 0, 0, 0}'}}};")
+        w(f"    __device__ const int {pre}AttachFine[{max(1, len(afine))}] = {{{', '.join(map(str, afine)) or '0'}}};")
         w(stg_if)
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         if True:
@@ -715,6 +740,24 @@ def gen_cuda(model: dict) -> str:
     for l in body:
         w("        " + l)
     w("    }")
+    w("")
+
+    # ---- end-effector transform and the attachment checks (fkcc_attach)
+    em = Emitter("cuda", SNAP32)
+    fr = frames_block(em)
+    vals = emit_ee_pose(em, fr, kin, model["end_effector"])
+    body = list(em.lines) + [" ".join(f"T[{i}] = {em.ref(v)};" for i, v in enumerate(vals))]
+    w(f"    // Transform of {model['end_effector']}, where fkcc_attach poses an attachment: R row-major, then t.")
+    w("    static __device__ __forceinline__ void ee_pose(const float *q, float *T)")
+    w("    {")
+    for l in body:
+        w("        " + l)
+    w("    }")
+    rows, afine = attach_tables(model, coarse_slot)
+    w("    // links checked against an attachment, in the reference's order: coarse slot, fine range")
+    w(f"    static constexpr int kAttachLinks = {len(rows)};")
+    w(f"    static __device__ __forceinline__ int4 attach_link(int i) {{ return k{S}AttachLink[i]; }}")
+    w(f"    static __device__ __forceinline__ int attach_fine(int i) {{ return k{S}AttachFine[i]; }}")
     w("")
 
     if tabled:
@@ -1250,6 +1293,11 @@ def gen_c(model: dict) -> str:
         for sa, sb in e["fine"]:
             self_fine += [sa, sb]
     self_start.append(len(self_fine) // 2)
+    arows, afine = attach_tables(model, coarse_slot)
+    w("#define VGO_%s_ATTACH_LINKS %d" % (P, len(arows)))
+    w("static const int vgo_%s_attach_coarse[] = {%s};" % (name, ", ".join(str(r[0]) for r in arows) or "0"))
+    w("static const int vgo_%s_attach_start[] = {%s};" % (name, ", ".join(str(r[1]) for r in arows + [(0, len(afine), 0)])))
+    w("static const int vgo_%s_attach_fine[] = {%s};" % (name, ", ".join(map(str, afine)) or "0"))
     w("#define VGO_%s_SELF_CHECKS %d" % (P, len(model["self_checks"])))
     w("static const int vgo_%s_self_coarse[] = {%s};" % (name, ", ".join(map(str, self_coarse)) or "0"))
     w("static const int vgo_%s_self_start[] = {%s};" % (name, ", ".join(map(str, self_start))))
@@ -1271,6 +1319,18 @@ def gen_c(model: dict) -> str:
             rr = lit32(r) if tgt == "c32" else lit64(f32(r))
             body.append(f"out[{4 * i}] = {em.ref(x)}; out[{4 * i + 1}] = {em.ref(y)}; out[{4 * i + 2}] = {em.ref(z)}; out[{4 * i + 3}] = {rr};")
         suffix = "f32" if tgt == "c32" else "f64"
+        if tgt == "c32":
+            em2 = Emitter(tgt, SNAP32)
+            fr2 = emit_frames(kin, em2, "q", sc_fn=scf)
+            vals = emit_ee_pose(em2, fr2, kin, model["end_effector"])
+            w(f"/* Transform of {model['end_effector']} (fkcc_attach's attachment frame): R row-major, then t. */")
+            w(f"static void vgo_{name}_ee_pose_f32(const float *q, float *T)")
+            w("{")
+            for l in em2.lines:
+                w("    " + l)
+            w("    " + " ".join(f"T[{i}] = {em2.ref(v)};" for i, v in enumerate(vals)))
+            w("}")
+            w("")
         w(f"/* Every sphere slot (fine, then coarse), {ty}: out[4 * slot + (x, y, z, r)]. */")
         w(f"static void vgo_{name}_spheres_{suffix}(const {ty} *q, {ty} *out)")
         w("{")

@@ -186,6 +186,29 @@ class _Lookup(dict):
         return self.env[k]
 
 
+def parse_attach(text: str) -> dict:
+    """The attachment checks of Robot::fkcc_attach (e.g. panda.hh:10265-15445): the frame the
+    attachment is posed at (the y slots of its transform) and, per robot link checked against
+    the attachment, its coarse slot and fine slots."""
+    body = _body(text, "inline static bool fkcc_attach(")
+    frame = re.search(r"//\s*attaching at (\S+)", body).group(1)
+    pose = int(re.search(r"set_attachment_pose\(environment, to_isometry\(&y\[(\d+)\]\)\)", body).group(1))
+    tail = body[body.index("attachment vs. robot collisions") :]
+    checks = []
+    for part in re.split(r"//\s*Attachment vs\. ", tail)[1:]:
+        link = part.split()[0]
+        slots = [int(m) // 4 for m in re.findall(r"attachment_sphere_collision<[^>]*>\(environment, y\[(\d+)\]", part)]
+        checks.append({"link": link, "coarse_slot": slots[0], "fine": slots[1:]})
+    return {"frame": frame, "pose_slot": pose, "checks": checks}
+
+
+def eefk_statements(text: str):
+    """FK statements of Robot::eefk (the end-effector transform, y[0..11])."""
+    body = _body(text, "inline static auto eefk(")
+    return [(t.strip(), " ".join(e.strip().rstrip(";").split()))
+            for t, e in re.findall(r"^\s*([vy]\[\d+\])\s*=\s*([^;]*;)", body, re.M)]
+
+
 # --------------------------------------------------------------------------------------------
 # model assembly
 
@@ -282,6 +305,22 @@ def build_model(reference: Path, robot: str, seed: int = 0) -> dict:
         for sa, sb in e["fine"]:
             assert fine[sa]["link"] == e["links"][0] and fine[sb]["link"] == e["links"][1]
 
+    # attachment checks (fkcc_attach): the pose frame is the end effector, whose transform the
+    # header's eefk computes (translation, then the rotation column-major, vector/math.hh:39-51)
+    att = parse_attach(hdr)
+    assert att["frame"] == consts["end_effector"], att["frame"]
+    ee_stmts = eefk_statements(hdr)
+    for q, tf in zip(samples, tfs):
+        y = evaluate(ee_stmts, q)
+        R, t = tf[att["frame"]]
+        assert np.abs(np.array([y[k] for k in range(3)]) - t).max() < 1e-9
+        assert np.abs(np.array([y[3 + k] for k in range(9)]).reshape(3, 3).T - R).max() < 1e-9
+    for c in att["checks"]:
+        assert coarse[c["link"]]["slot"] == c["coarse_slot"], c["link"]
+        for s_ in c["fine"]:
+            assert fine[s_]["link"] == c["link"], (s_, c["link"])
+    attach_checks = [{"link": c["link"], "fine": c["fine"]} for c in att["checks"]]
+
     joints = []
     for j in urdf.joints:
         joints.append(
@@ -312,6 +351,7 @@ def build_model(reference: Path, robot: str, seed: int = 0) -> dict:
         "coarse_spheres": {k: {"p": v["p"], "r": v["r"]} for k, v in coarse.items()},
         "env_checks": env_checks,
         "self_checks": self_checks,
+        "attach_checks": attach_checks,
         "source": {
             "urdf": f"resources/{robot}/{robot}_spherized.urdf",
             "header": f"src/impl/vamp/robots/{robot}.hh",
