@@ -103,6 +103,12 @@ int vg_filter_pointcloud(const float *xyz, size_t n, float min_dist, float max_r
  * sizes. */
 int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, float *tests, float *aabbs,
                              uint32_t *aff_starts, float *aff, float *top);
+/* A heightfield (collision/shapes.hh:250-311; factory heightfield::flat, collision/factory.hh:
+ * 365-386; Environment.add_heightfield, bindings/environment.cc:146-149): xd x yd samples
+ * (data[y * xd + x]), placed at centre[3], cells scale[0] x scale[1], heights data / scale[2] +
+ * centre[2].  Checked by sphere_heightfield (collision/sphere_heightfield.hh:9-30) in every
+ * environment query.  At most 8 per environment and 2^24 samples each. */
+int vg_env_add_heightfield(vg_env *env, const float *centre, const float *scale, size_t xd, size_t yd, const float *data);
 /* An attachment (collision/attachments.hh:11-56; Environment.attach / detach,
  * bindings/environment.cc:162-165; vamp.Attachment, :200-230): k spheres {x, y, z, r} in a frame
  * at the row-major 4x4 transform tf16 from the robot's end effector.  The environment copies

@@ -61,6 +61,14 @@ struct vgo_env
     vgo_capt *clouds[VGO_MAX_CLOUDS];
     int n_clouds;
     int sqrt_mode;
+    /* heightfields (collision/shapes.hh:250-311): offsets, inverted scales, sizes, data */
+    struct
+    {
+        float x, y, z, xs, ys, zs;
+        int xd, yd, id;
+        float *data;
+    } hf[VGO_MAX_HEIGHTFIELDS];
+    int n_hf;
     /* attachment: relative transform rows {R[r][0], R[r][1], R[r][2], t[r]}, then spheres */
     int n_att; /* -1: none attached */
     float att[12 + 4 * VGO_MAX_ATTACH];
@@ -72,6 +80,26 @@ vgo_env *vgo_env_create(void)
     e->sqrt_mode = VGO_SQRT_X86;
     e->n_att = -1;
     return e;
+}
+
+int vgo_env_add_heightfield(vgo_env *e, const float *centre, const float *scale, int xd, int yd, const float *data)
+{
+    if (e->n_hf >= VGO_MAX_HEIGHTFIELDS || xd <= 0 || yd <= 0)
+        return -1;
+    const int i = e->n_hf++;
+    e->hf[i].x = centre[0];
+    e->hf[i].y = centre[1];
+    e->hf[i].z = centre[2];
+    /* heightfield::flat stores the inverted scales (collision/factory.hh:376-385) */
+    e->hf[i].xs = 1.0f / scale[0];
+    e->hf[i].ys = 1.0f / scale[1];
+    e->hf[i].zs = 1.0f / scale[2];
+    e->hf[i].xd = xd;
+    e->hf[i].yd = yd;
+    e->hf[i].id = e->n_added++;
+    e->hf[i].data = (float *)malloc((size_t)xd * yd * sizeof(float));
+    memcpy(e->hf[i].data, data, (size_t)xd * yd * sizeof(float));
+    return 0;
 }
 
 int vgo_env_attach(vgo_env *e, const float *tf16, const float *spheres, int k)
@@ -102,6 +130,8 @@ void vgo_env_destroy(vgo_env *e)
     }
     for (int i = 0; i < e->n_clouds; ++i)
         vgo_capt_destroy(e->clouds[i]);
+    for (int i = 0; i < e->n_hf; ++i)
+        free(e->hf[i].data);
     free(e);
 }
 
@@ -271,6 +301,28 @@ static inline float t_zcuboid(const float *o, float x, float y, float z, float r
     return fmaf(a3, a3, fmaf(a2, a2, a1 * a1)) - rsq;
 }
 
+/* sphere_heightfield (collision/sphere_heightfield.hh:9-30): the cell under the sphere centre,
+ * floor(clamp(xs * (x0 - x) + xd / 2, 0, xd)) (one fused multiply-add, as the reference's x86-64
+ * build computes it) and the same in y, index y * xd + x; the test value z - r - (zs * h + z0),
+ * which that build reassociates to fma(-zs, h, (z - r) - z0) (found by comparing with the
+ * compiled reference).  The reference reads past its data for centres beyond the far edges
+ * (index >= xd * yd); here the index is clamped to the last cell there. */
+static float clamp_ps(float v, float lo, float hi)
+{
+    const float m = v > lo ? v : lo; /* _mm256_max_ps(v, lo), then _mm256_min_ps(m, hi) */
+    return m < hi ? m : hi;
+}
+
+static float t_heightfield(const vgo_env *e, int i, float x, float y, float z, float r)
+{
+    const float X = floorf(clamp_ps(fmaf(e->hf[i].xs, e->hf[i].x - x, (float)(e->hf[i].xd / 2)), 0.0f, (float)e->hf[i].xd));
+    const float Y = floorf(clamp_ps(fmaf(e->hf[i].ys, e->hf[i].y - y, (float)(e->hf[i].yd / 2)), 0.0f, (float)e->hf[i].yd));
+    long idx = (long)fmaf(Y, (float)e->hf[i].xd, X);
+    const long last = (long)e->hf[i].xd * e->hf[i].yd - 1;
+    idx = idx < 0 ? 0 : (idx > last ? last : idx);
+    return fmaf(-e->hf[i].zs, e->hf[i].data[idx], (z - r) - e->hf[i].z);
+}
+
 /* ============================================================ sphere vs environment (block) */
 
 /* sphere_environment_in_collision (validity.hh:47-150) for one block of `lanes` spheres:
@@ -308,6 +360,14 @@ int vgo_sphere_env(const vgo_env *e, int lanes, const float *x, const float *y, 
     VGO_KIND_LOOP(2, t_zcapsule, r)
     VGO_KIND_LOOP(3, t_cuboid, rsq)
     VGO_KIND_LOOP(4, t_zcuboid, rsq)
+    for (int i = 0; i < e->n_hf; ++i)
+    {
+        int hit = 0;
+        for (int l = 0; l < lanes; ++l)
+            hit |= vgo_signbit(t_heightfield(e, i, x[l], y[l], z[l], r[l]));
+        if (hit)
+            return 1;
+    }
     for (int c = 0; c < e->n_clouds; ++c)
     {
         g_cnt.capt_queries += (uint64_t)lanes;
@@ -348,6 +408,11 @@ static void debug_sphere(const vgo_env *e, float x, float y, float z, float r, u
     VGO_DEBUG_KIND(3, t_cuboid, rsq)
     VGO_DEBUG_KIND(4, t_zcuboid, rsq)
 #undef VGO_DEBUG_KIND
+    for (int i = 0; i < e->n_hf; ++i)
+    {
+        if (vgo_signbit(t_heightfield(e, i, x, y, z, r)))
+            bits[e->hf[i].id >> 5] |= 1u << (e->hf[i].id & 31);
+    }
 }
 
 const struct vgo_capt *vgo_env_capt(const vgo_env *e, int idx)

@@ -39,6 +39,10 @@ void vgo_env_set_sqrt_mode(vgo_env *e, int mode); /* VGO_SQRT_X86 (default) or V
  * in a frame at the relative transform tf (4x4, row-major) from the end effector; checked by
  * fkcc_attach.  Returns 0 on success (k <= VGO_MAX_ATTACH). */
 #define VGO_MAX_ATTACH 64
+/* heightfield (collision/shapes.hh:250-311; factory heightfield::flat, factory.hh:365-386):
+ * centre offsets, scales (stored inverted), xd x yd samples; returns 0 on success */
+#define VGO_MAX_HEIGHTFIELDS 8
+int vgo_env_add_heightfield(vgo_env *e, const float *centre, const float *scale, int xd, int yd, const float *data);
 int vgo_env_attach(vgo_env *e, const float *tf16, const float *spheres, int k);
 void vgo_env_detach(vgo_env *e);
 /* end-effector transform of one configuration: R row-major (9), then t (3) (Robot::eefk) */

@@ -85,6 +85,21 @@ int vgref_env_add_pointcloud(void *h, const float *pts, size_t n, float r_min, f
     return 0;
 }
 
+// A heightfield with data [xd * yd], named by insertion order like the primitives.  Built with the
+// reference's HeightField constructor (collision/shapes.hh:270-294) and the arguments its factory
+// passes (collision/factory.hh:365-386, heightfield::flat: the scales inverted); factory.hh itself
+// needs Eigen, which the stand-in does not provide.
+void vgref_env_add_heightfield(void *h, const float *centre, const float *scale, size_t xd, size_t yd,
+                               const float *data)
+{
+    auto *e = static_cast<RefEnv *>(h);
+    HeightField<float> hf(centre[0], centre[1], centre[2], 1.F / scale[0], 1.F / scale[1], 1.F / scale[2], xd, yd,
+                          std::vector<float>(data, data + xd * yd));
+    hf.name = std::to_string(e->n_added++);
+    e->scalar.heightfields.emplace_back(hf);
+    e->dirty = true;
+}
+
 // Sorts each primitive list by min_distance and builds the 8-lane environment, as the reference's
 // Python binding does before every query (bindings/environment.cc, bindings/robot_helper.hh:252).
 void vgref_env_finalize(void *h)

@@ -140,6 +140,7 @@ class Port:
         lib.vgo_env_total.argtypes = [_p]
         lib.vgo_robot_self_pairs.argtypes = [_p]
         lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
+        lib.vgo_env_add_heightfield.argtypes = [_p, _p, _p, ctypes.c_int, ctypes.c_int, _p]
         lib.vgo_env_attach.argtypes = [_p, _p, _p, ctypes.c_int]
         lib.vgo_env_detach.argtypes = [_p]
         lib.vgo_robot_ee_pose.argtypes = [_p, _p, _p]
@@ -246,6 +247,11 @@ class PortEnv:
             rc = lib.vgo_env_add_pointcloud(self.h, _ptr(pts), len(pts), pc["r_min"], pc["r_max"], pc["r_point"])
             if rc:
                 raise RuntimeError("pointcloud rejected")
+        for hf in scene.get("heightfields", []):
+            c, sc = (np.ascontiguousarray(hf[k], np.float32) for k in ("centre", "scale"))
+            data = np.ascontiguousarray(hf["data"], np.float32)
+            if lib.vgo_env_add_heightfield(self.h, _ptr(c), _ptr(sc), int(hf["xd"]), int(hf["yd"]), _ptr(data)):
+                raise RuntimeError("heightfield rejected")
         if scene.get("attachment") is not None:
             tf = np.ascontiguousarray(scene["attachment"]["tf"], np.float32).reshape(16)
             sph = np.ascontiguousarray(scene["attachment"]["spheres"], np.float32).reshape(-1, 4)
@@ -265,6 +271,15 @@ class PortEnv:
         out = np.zeros((n, width), np.float32)
         for i in range(n):
             lib.vgo_env_get(self.h, kind, i, _ptr(out[i]))
+        return out
+
+    def sphere_env(self, spheres: np.ndarray, lanes: int = 8) -> np.ndarray:
+        """sphere_environment_in_collision per block of `lanes` spheres [n, 4] (1 = collides)."""
+        s = np.ascontiguousarray(spheres, np.float32).reshape(-1, lanes, 4)
+        out = np.zeros(len(s), np.uint8)
+        for i, b in enumerate(s):
+            cols = [np.ascontiguousarray(b[:, k]) for k in range(4)]
+            out[i] = self.port.lib.vgo_sphere_env(self.h, lanes, *(_ptr(c) for c in cols))
         return out
 
     def validate_states(self, robot: PortRobot, q: np.ndarray, threads: int = 1) -> np.ndarray:
@@ -346,6 +361,7 @@ class Reference:
         lib.vgref_vec_sqrt8.argtypes = [_p, _p]
         lib.vgref_vec_sincos8.argtypes = [_p, _p, _p]
         lib.vgref_sphere_env8.argtypes = [_p, _p, _p, _p, _p]
+        lib.vgref_env_add_heightfield.argtypes = [_p, _p, _p, _sz, _sz, _p]
         for r in ("panda", "ur5", "fetch", "baxter"):
             getattr(lib, f"vgref_{r}_info").argtypes = [_p, _p, _p, _p, _p]
             getattr(lib, f"vgref_{r}_limits").argtypes = [_p, _p]
@@ -418,7 +434,20 @@ class RefEnv:
         for pc in scene.get("pointclouds", []):
             pts = np.ascontiguousarray(pc["points"], np.float32)
             lib.vgref_env_add_pointcloud(self.h, _ptr(pts), len(pts), pc["r_min"], pc["r_max"], pc["r_point"])
+        for hf in scene.get("heightfields", []):
+            c, sc = (np.ascontiguousarray(hf[k], np.float32) for k in ("centre", "scale"))
+            data = np.ascontiguousarray(hf["data"], np.float32)
+            lib.vgref_env_add_heightfield(self.h, _ptr(c), _ptr(sc), int(hf["xd"]), int(hf["yd"]), _ptr(data))
         lib.vgref_env_finalize(self.h)
+
+    def sphere_env(self, spheres: np.ndarray) -> np.ndarray:
+        """The reference's sphere_environment_in_collision per 8-lane block of spheres [n, 4]."""
+        s = np.ascontiguousarray(spheres, np.float32).reshape(-1, 8, 4)
+        out = np.zeros(len(s), np.uint8)
+        for i, b in enumerate(s):
+            cols = [np.ascontiguousarray(b[:, k]) for k in range(4)]
+            out[i] = self.ref.lib.vgref_sphere_env8(self.h, *(_ptr(c) for c in cols))
+        return out
 
     def __del__(self):
         try:

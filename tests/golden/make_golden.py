@@ -86,10 +86,34 @@ def eefk_fixtures(reference: Path) -> None:
         np.savez_compressed(OUT / f"eefk_{r}.npz", q=q, T=T)
 
 
+def heightfield_fixtures(ref: Reference) -> None:
+    """The heightfield primitive (collision/sphere_heightfield.hh:9-30) in the reference's
+    sphere_environment_in_collision: blocks of one sphere repeated (single-sphere verdicts) and of
+    8 different spheres, all over the grid's valid cells; and Panda configurations above the
+    terrain (Robot::fkcc through validate)."""
+    rng = np.random.default_rng(91)
+    hf = scenes.heightfield(92)
+    scene = {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+             "cuboids": np.zeros((0, 15), np.float32), "heightfields": [hf]}
+    n = 2000
+    one = np.stack([rng.uniform(-0.9, 1.2, n), rng.uniform(-1.1, 1.2, n), rng.uniform(-0.2, 0.35, n),
+                    rng.uniform(0.01, 0.1, n)], 1).astype(np.float32)
+    mixed = np.stack([rng.uniform(-0.9, 1.2, 8 * 400), rng.uniform(-1.1, 1.2, 8 * 400),
+                      rng.uniform(0.0, 0.35, 8 * 400), rng.uniform(0.01, 0.05, 8 * 400)], 1).astype(np.float32)
+    renv = ref.env(scene)
+    rb = Port().robot("panda")
+    q = scenes.configurations(rb.s_m, rb.s_a, 1024, 93)
+    np.savez_compressed(OUT / "heightfield.npz", centre=hf["centre"], scale=hf["scale"], xd=hf["xd"], yd=hf["yd"],
+                        data=hf["data"], single=one, single_verdict=renv.sphere_env(np.repeat(one, 8, axis=0)),
+                        mixed=mixed, mixed_verdict=renv.sphere_env(mixed), q=q,
+                        state_verdict=renv.validate_states("panda", q))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None)
-    ap.add_argument("--only", choices=["filter", "eefk"], default=None, help="regenerate one group of fixtures")
+    ap.add_argument("--only", choices=["filter", "eefk", "heightfield"], default=None,
+                    help="regenerate one group of fixtures")
     a = ap.parse_args()
     if build_reference(a.reference) is None:
         raise SystemExit("reference checkout not found (or not x86-64): cannot generate golden fixtures")
@@ -99,6 +123,8 @@ def main():
         filter_fixtures(ref)
     if a.only in (None, "eefk"):
         eefk_fixtures(Path(a.reference or "/root/reference"))
+    if a.only in (None, "heightfield"):
+        heightfield_fixtures(ref)
     if a.only is not None:
         return
 

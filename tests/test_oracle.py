@@ -223,3 +223,21 @@ def test_attachment_checks_in_the_oracle(port):
     self_only = port.env(_attach_scene(empty, [[0, 0, 0, 0.25]], offset=0.0)).validate_states(rb, q)
     plain_empty = port.env(empty).validate_states(rb, q)
     assert (plain_empty & ~self_only).any()
+
+
+def _hf_scene(g: dict) -> dict:
+    hf = {"centre": g["centre"], "scale": g["scale"], "xd": int(g["xd"]), "yd": int(g["yd"]), "data": g["data"]}
+    return {"spheres": np.zeros((0, 4), np.float32), "capsules": np.zeros((0, 8), np.float32),
+            "cuboids": np.zeros((0, 15), np.float32), "heightfields": [hf]}
+
+
+def test_heightfield_matches_the_reference(port):
+    """sphere_heightfield (collision/sphere_heightfield.hh:9-30) inside
+    sphere_environment_in_collision, and Panda states above the terrain (golden fixture from the
+    compiled reference)."""
+    g = golden("heightfield")
+    env = port.env(_hf_scene(g))
+    assert np.array_equal(env.sphere_env(np.repeat(g["single"], 8, axis=0)), g["single_verdict"])
+    assert np.array_equal(env.sphere_env(g["mixed"]), g["mixed_verdict"])
+    assert np.array_equal(env.validate_states(port.robot("panda"), g["q"]), g["state_verdict"])
+    assert 0.1 < g["single_verdict"].mean() < 0.9 and 0.1 < g["state_verdict"].mean() < 0.95

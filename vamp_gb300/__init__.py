@@ -16,7 +16,7 @@ from __future__ import annotations
 
 _API = {"Environment", "Robot", "VampError", "SQRT_X86", "SQRT_EXACT", "panda", "ur5", "fetch", "baxter", "ROBOTS",
         "autotune", "Batch", "CollisionPredictor", "SCHEDULES", "filter_pointcloud", "filter_pointcloud_device",
-        "Attachment"}
+        "Attachment", "HeightField", "make_heightfield", "array_to_heightfield"}
 
 
 def __getattr__(name):

@@ -98,6 +98,8 @@ class Environment:
             env.add_cuboid(c)
         for pc in scene.get("pointclouds", []):
             env.add_pointcloud(pc["points"], pc["r_min"], pc["r_max"], pc["r_point"])
+        for hf in scene.get("heightfields", []):
+            env.add_heightfield(HeightField(hf["centre"], hf["scale"], (hf["xd"], hf["yd"]), hf["data"]))
         if scene.get("attachment") is not None:
             a = Attachment(scene["attachment"]["tf"])
             a.add_spheres(np.asarray(scene["attachment"]["spheres"], np.float32).reshape(-1, 4))
@@ -120,6 +122,16 @@ class Environment:
         with torch.cuda.device(pts.device):
             check(lib.vg_env_add_pointcloud_device(self._h, pts.data_ptr(), pts.shape[0], float(r_min), float(r_max),
                                                    float(r_point), _stream(pts)))
+
+    def add_heightfield(self, heightfield: "HeightField") -> None:
+        """Environment.add_heightfield (bindings/environment.cc:146-149)."""
+        h = heightfield
+        c, sc = (np.ascontiguousarray(v, np.float32).reshape(3) for v in (h.centre, h.scale))
+        data = np.ascontiguousarray(h.data, np.float32).reshape(-1)
+        xd, yd = (int(v) for v in h.dimensions)
+        if data.size != xd * yd:
+            raise ValueError("heightfield data must hold dimensions[0] * dimensions[1] samples")
+        check(lib.vg_env_add_heightfield(self._h, _ptr(c), _ptr(sc), xd, yd, _ptr(data)))
 
     def attach(self, attachment: "Attachment") -> None:
         """Attach spheres to the end effector (Environment.attach, bindings/environment.cc:162-164):
@@ -339,6 +351,30 @@ def _stream(t):
     import torch
 
     return torch.cuda.current_stream(t.device).cuda_stream
+
+
+class HeightField:
+    """A heightfield (collision/shapes.hh:250-311): samples data[y * xd + x] for dimensions
+    (xd, yd), placed at `centre`; scale holds the cell sizes in x and y and the divisor of the
+    samples in z (as the reference's make_heightfield takes them)."""
+
+    def __init__(self, centre, scale, dimensions, data):
+        self.centre = np.asarray(centre, np.float32).reshape(3)
+        self.scale = np.asarray(scale, np.float32).reshape(3)
+        self.dimensions = (int(dimensions[0]), int(dimensions[1]))
+        self.data = np.asarray(data, np.float32).reshape(-1)
+
+
+def make_heightfield(center, scale, dimensions, data) -> HeightField:
+    """make_heightfield (bindings/environment.cc:98; collision/factory.hh:406-422)."""
+    return HeightField(center, scale, dimensions, data)
+
+
+def array_to_heightfield(array, center, scaling) -> HeightField:
+    """png_to_heightfield (src/vamp/__init__.py:54-66) after the image is decoded: a grey image
+    [rows, cols] of 0..255, scaled to [0, 1] and flipped upside down."""
+    a = np.flip(np.asarray(array, np.float64) * 1 / 255.0, axis=0)
+    return make_heightfield(center, scaling, a.shape, a.reshape(-1))
 
 
 class Attachment:

@@ -237,9 +237,28 @@ namespace vg
         }
         if (int rc = upload_clouds(e))
             return rc;
+        // heightfield samples: one device buffer each, uploaded once
+        while (e->d_hf.size() < e->hf.size())
+        {
+            const std::vector<float> &h = e->hf_data[e->d_hf.size()];
+            void *p = nullptr;
+            VG_CUDA(cudaMalloc(&p, h.size() * sizeof(float)), "cudaMalloc(heightfield)");
+            e->d_hf.push_back(p);
+            VG_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice), "upload heightfield");
+        }
         std::vector<float4> img;
         pack_image(e, img, e->off, e->n);
         pack_clouds(e, img, &e->cloud_off);
+        static_assert(sizeof(HeightView) % sizeof(float4) == 0, "HeightView must pack into float4s");
+        e->hf_off = static_cast<int>(img.size());
+        for (size_t i = 0; i < e->hf.size(); ++i)
+        {
+            HeightView v = e->hf[i];
+            v.data = static_cast<const float *>(e->d_hf[i]);
+            const size_t at = img.size();
+            img.resize(at + sizeof(HeightView) / sizeof(float4));
+            std::memcpy(&img[at], &v, sizeof(HeightView));
+        }
         // the attachment: 3 transform rows, then its spheres
         e->att_off = static_cast<int>(img.size());
         if (e->n_att >= 0)
@@ -284,6 +303,8 @@ namespace vg
         d.cloud_off = e->cloud_off;
         d.n_att = e->n_att;
         d.att_off = e->att_off;
+        d.n_hf = static_cast<int>(e->hf.size());
+        d.hf_off = e->hf_off;
         return d;
     }
 
@@ -356,13 +377,14 @@ namespace vg
         const vg_env *env = m.env;
         const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
         const int which = env->lanes == 8 ? 0 : 1;
-        // with an attachment every schedule runs fkcc_attach in the segment-per-edge kernel (the
-        // block order does not change verdicts, so a learned order is not needed there)
-        const bool attach = env->n_att >= 0;
-        const bool learned = !attach && m.scores != nullptr;
-        const bool grouped = !attach && (learned || m.schedule >= 1);
+        // with heightfields or an attachment every schedule runs the extended checks in the
+        // segment-per-edge kernel (the block order does not change verdicts, so a learned order
+        // is not needed there)
+        const bool ext = env->extended();
+        const bool learned = !ext && m.scores != nullptr;
+        const bool grouped = !ext && (learned || m.schedule >= 1);
         const bool wide = grouped && !learned && m.schedule == 2;
-        const void *fn = attach ? r->edges_attach_fn[which]
+        const void *fn = ext ? r->edges_ext_fn[which]
                                 : learned ? r->edges_learned_fn[which]
                                           : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
         int occ = 0;
@@ -377,7 +399,7 @@ namespace vg
         const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
         const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
         EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes};
-        const auto launch = attach ? r->edges_attach[which]
+        const auto launch = ext ? r->edges_ext[which]
                                    : learned ? r->edges_learned[which]
                                              : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
         VG_CUDA(launch(p, grid, kBlock, smem, s), "edges kernel launch");
@@ -495,6 +517,8 @@ void vg_env_destroy(vg_env *env)
     if (env->d_stage)
         cudaFree(env->d_stage);
     for (void *p : env->d_clouds)
+        cudaFree(p);
+    for (void *p : env->d_hf)
         cudaFree(p);
     delete env;
 }
@@ -685,15 +709,40 @@ int vg_validate_states_device(const char *robot, vg_env *env, const float *q, si
     if (int rc = commit(env))
         return rc;
     const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    const bool attach = env->n_att >= 0;
+    const bool ext = env->extended();
     int occ = 0;
-    if (int rc = prepare_kernel(attach ? r->states_attach_fn : r->states_fn, smem, kBlock, &occ))
+    if (int rc = prepare_kernel(ext ? r->states_ext_fn : r->states_fn, smem, kBlock, &occ))
         return rc;
     const long long want = (static_cast<long long>(n) + kBlock - 1) / kBlock;
     const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
     StatesParams p{q, static_cast<long long>(n), out, env_device(env)};
-    VG_CUDA((attach ? r->states_attach : r->states)(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)),
+    VG_CUDA((ext ? r->states_ext : r->states)(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)),
             "states kernel launch");
+    return VG_OK;
+}
+
+int vg_env_add_heightfield(vg_env *env, const float *centre, const float *scale, size_t xd, size_t yd, const float *data)
+{
+    if (!env || !centre || !scale || !data || xd == 0 || yd == 0)
+        return set_error(VG_ERR_ARG, "vg_env_add_heightfield: null argument or empty grid");
+    if (env->hf.size() >= static_cast<size_t>(kMaxHeightfields))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_heightfield: at most 8 heightfields per environment");
+    if (xd * yd >= (size_t{1} << 24))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_heightfield: at most 2^24 samples (cell indices are exact in FP32)");
+    HeightView v{};
+    v.x = centre[0];
+    v.y = centre[1];
+    v.z = centre[2];
+    // heightfield::flat stores the inverted scales (collision/factory.hh:376-385)
+    v.xs = 1.0f / scale[0];
+    v.ys = 1.0f / scale[1];
+    v.zs = 1.0f / scale[2];
+    v.xd = static_cast<int>(xd);
+    v.yd = static_cast<int>(yd);
+    v.id = env->n_added++;
+    env->hf.push_back(v);
+    env->hf_data.emplace_back(data, data + xd * yd);
+    env->dirty = true;
     return VG_OK;
 }
 

@@ -183,6 +183,19 @@ namespace vg
     };
     constexpr int kMaxClouds = 4;
 
+    // One heightfield (collision/shapes.hh:250-311) on the device: offsets, inverted scales
+    // (collision/factory.hh:376-385), grid size, samples [xd * yd] in global memory, and its
+    // insertion id (debug reports).
+    struct HeightView
+    {
+        float x, y, z, xs, ys, zs;
+        int xd, yd;
+        const float *data;
+        int id;
+        int pad;
+    };
+    constexpr int kMaxHeightfields = 8;
+
     struct EnvView
     {
         const float4 *rec[5];
@@ -193,7 +206,27 @@ namespace vg
         int n_clouds;
         const float4 *att;  // attachment: 3 transform rows {R[r][0..2], t[r]}, then spheres
         int n_att;          // -1: none
+        const HeightView *hf;
+        int n_hf;
     };
+
+    // sphere_heightfield (collision/sphere_heightfield.hh:9-30), sign bit set iff the sphere is
+    // below the surface: the cell floor(clamp(xs * (x0 - x) + xd / 2, 0, xd)) (one fused
+    // multiply-add) and the same in y, index y * xd + x, and the value z - r - (zs * h + z0) as
+    // the reference's x86-64 build reassociates it, fma(-zs, h, (z - r) - z0).  Centres beyond
+    // the far edges (where the reference reads past its samples) use the last cell.
+    __device__ __forceinline__ float t_heightfield(const HeightView &h, float x, float y, float z, float r)
+    {
+        const float fx = __fmaf_rn(h.xs, __fsub_rn(h.x, x), static_cast<float>(h.xd / 2));
+        const float fy = __fmaf_rn(h.ys, __fsub_rn(h.y, y), static_cast<float>(h.yd / 2));
+        const float mx = fx > 0.0f ? fx : 0.0f, my = fy > 0.0f ? fy : 0.0f;  // max(v, 0), NaN to 0
+        const float cx = floorf(mx < static_cast<float>(h.xd) ? mx : static_cast<float>(h.xd));
+        const float cy = floorf(my < static_cast<float>(h.yd) ? my : static_cast<float>(h.yd));
+        long long idx = static_cast<long long>(__fmaf_rn(cy, static_cast<float>(h.xd), cx));
+        const long long last = static_cast<long long>(h.xd) * h.yd - 1;
+        idx = idx < 0 ? 0 : (idx > last ? last : idx);
+        return __fmaf_rn(-h.zs, __ldg(h.data + idx), __fsub_rn(__fsub_rn(z, r), h.z));
+    }
 
     __device__ __forceinline__ float sql2(float ax, float ay, float az, float bx, float by, float bz)
     {
@@ -476,7 +509,9 @@ namespace vg
     // sphere_environment_in_collision (validity.hh:47-150) for NS spheres at once, each over the
     // segments in `mask`.  hit[s] receives the lanes of the segments whose block collides for
     // sphere s.  Warp-uniform; all 32 lanes must call.
-    template <int W, int NS>
+    // kExt: also the heightfields (kernels built for environments with heightfields or an
+    // attachment; the default kernels leave them out)
+    template <int W, int NS, bool kExt = false>
     __device__ __forceinline__ void env_multi(const EnvView &e, const float4 *sph, unsigned mask, unsigned *hit)
     {
         const int lane = threadIdx.x & 31;
@@ -507,6 +542,18 @@ namespace vg
         kind_pass<2, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
         kind_pass<3, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
         kind_pass<4, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
+        if constexpr (kExt)
+        {
+#pragma unroll 1
+            for (int h = 0; h < e.n_hf; ++h)
+            {
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+                {
+                    bits[s] |= __float_as_uint(t_heightfield(e.hf[h], x[s], y[s], z[s], r[s]));
+                }
+            }
+        }
 #pragma unroll
         for (int s = 0; s < NS; ++s)
         {
@@ -552,32 +599,32 @@ namespace vg
     }
 
     // Single-sphere query, inlined into the caller.
-    template <int W>
+    template <int W, bool kExt = false>
     __device__ __forceinline__ unsigned env_query_inline(const EnvView &e, float x, float y, float z, float r, unsigned mask)
     {
         const float4 s = make_float4(x, y, z, r);
         unsigned hit;
-        env_multi<W, 1>(e, &s, mask, &hit);
+        env_multi<W, 1, kExt>(e, &s, mask, &hit);
         return hit;
     }
 
     // Single-sphere form.
-    template <int W>
+    template <int W, bool kExt = false>
     __device__ __noinline__ unsigned env_query(const EnvView &e, float x, float y, float z, float r, unsigned mask)
     {
         const float4 s = make_float4(x, y, z, r);
         unsigned hit;
-        env_multi<W, 1>(e, &s, mask, &hit);
+        env_multi<W, 1, kExt>(e, &s, mask, &hit);
         return hit;
     }
 
     // Fine tests of one link's NS spheres (one function per distinct NS): the segments in `mask`
     // whose block collides for any of the spheres.
-    template <int W, int NS>
+    template <int W, int NS, bool kExt = false>
     __device__ __noinline__ unsigned env_any(const EnvView &e, const float4 *sph, unsigned mask)
     {
         unsigned hit[NS];
-        env_multi<W, NS>(e, sph, mask, hit);
+        env_multi<W, NS, kExt>(e, sph, mask, hit);
         unsigned any = 0;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
@@ -609,11 +656,13 @@ namespace vg
     // words of per-warp shared scratch available to a generated fkcc (environment checks per robot)
     constexpr int kWarpScratch = 64;
 
-    // The context a generated Robot::fkcc body runs against.
-    template <int W>
+    // The context a generated Robot::fkcc body runs against.  kExt: the environment queries also
+    // test heightfields.
+    template <int W, bool kExtended = false>
     struct CheckCtx
     {
         static constexpr int kW = W;
+        static constexpr bool kExt = kExtended;
         const EnvView &env;
         unsigned alive;
         // every active lane's configuration lies inside the joint limits widened by the culling
@@ -626,19 +675,19 @@ namespace vg
 
         __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
         {
-            return env_query<W>(env, x, y, z, r, mask);
+            return env_query<W, kExt>(env, x, y, z, r, mask);
         }
 
         template <int NS>
         __device__ __forceinline__ void env_many(const float4 *s, unsigned mask, unsigned *hit)
         {
-            env_multi<W, NS>(env, s, mask, hit);
+            env_multi<W, NS, kExt>(env, s, mask, hit);
         }
 
         template <int NS>
         __device__ __forceinline__ unsigned env_any_hit(const float4 *s, unsigned mask)
         {
-            return env_any<W, NS>(env, s, mask);
+            return env_any<W, NS, kExt>(env, s, mask);
         }
 
         __device__ __forceinline__ unsigned self_hit(

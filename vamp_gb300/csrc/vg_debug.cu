@@ -78,6 +78,15 @@ namespace vg
         debug_kind<2>(ev, p.ids + p.id_off[2], x, y, z, r, rsq, me, bits);
         debug_kind<3>(ev, p.ids + p.id_off[3], x, y, z, r, rsq, me, bits);
         debug_kind<4>(ev, p.ids + p.id_off[4], x, y, z, r, rsq, me, bits);
+        // heightfields (validity.hh:240-246): every one, no distance cut-off
+        const HeightView *hf = reinterpret_cast<const HeightView *>(p.env.buf + p.env.hf_off);
+        for (int h = 0; h < p.env.n_hf; ++h)
+        {
+            if (__float_as_uint(t_heightfield(hf[h], x, y, z, r)) >> 31)
+            {
+                bits[hf[h].id >> 5] |= 1u << (hf[h].id & 31);
+            }
+        }
     }
 
 }  // namespace vg

@@ -34,11 +34,12 @@ namespace vg
         // same-edge schedule in a learned block order (EdgesParams::scores)
         cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_learned_fn[2];
-        // fkcc_attach forms (an attachment in the environment): states, and edges a segment each
-        cudaError_t (*states_attach)(const StatesParams &, int grid, int block, int smem, cudaStream_t);
-        const void *states_attach_fn;
-        cudaError_t (*edges_attach[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
-        const void *edges_attach_fn[2];
+        // extended forms (heightfields in the environment, or an attachment: fkcc_attach): states,
+        // and edges a segment each
+        cudaError_t (*states_ext)(const StatesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *states_ext_fn;
+        cudaError_t (*edges_ext[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_ext_fn[2];
         // Robot::eefk: row-major 4x4 transforms [n][16] from configurations [n][dim]
         cudaError_t (*ee_pose)(const float *, long long, float *, cudaStream_t);
         int stage_floats;  // shared-memory staging floats per thread (after the environment image)
@@ -101,6 +102,14 @@ struct vg_env
     int n_att = -1;
     std::vector<float> att;
     int att_off = 0;
+    // heightfields (vg_env_add_heightfield): descriptors (data pointer filled at upload), host
+    // samples, one device buffer each
+    std::vector<vg::HeightView> hf;
+    std::vector<std::vector<float>> hf_data;
+    std::vector<void *> d_hf;
+    int hf_off = 0;
+    // environments with heightfields or an attachment run the extended kernels
+    bool extended() const { return n_att >= 0 || !hf.empty(); }
     int n[5] = {0, 0, 0, 0, 0};
     // pointclouds: host trees and their device copies (tests, aabbs, starts, aff per cloud)
     std::vector<vg::CaptHost> clouds;

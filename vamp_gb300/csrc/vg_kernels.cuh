@@ -44,6 +44,8 @@ namespace vg
         int cloud_off;      // their offset, in float4
         int n_att;          // attachment spheres (-1: no attachment)
         int att_off;        // attachment block: 3 transform rows, then the spheres, in float4
+        int n_hf;           // HeightView descriptors
+        int hf_off;         // their offset, in float4
     };
 
     constexpr int kRsqrtF4 = 2048 / 4;
@@ -71,6 +73,8 @@ namespace vg
         v.n_clouds = d.n_clouds;
         v.att = smem + d.att_off - kRsqrtF4;
         v.n_att = d.n_att;
+        v.hf = reinterpret_cast<const HeightView *>(smem + d.hf_off - kRsqrtF4);
+        v.n_hf = d.n_hf;
         for (int k = 0; k < 5; ++k)
         {
             v.rec[k] = smem + d.off[k] - kRsqrtF4;
@@ -86,10 +90,10 @@ namespace vg
     // reference lists, its coarse sphere gating its fine spheres against the posed spheres
     // (attachment_sphere_collision, validity.hh:270-293).  Returns the segments still valid.
     // Every product is a chain of fused multiply-adds, first term first.
-    template <typename Robot, int W>
+    template <typename Robot, int W, bool kExt>
     __device__ __noinline__ unsigned attach_check(const EnvView &ev, const float *q, unsigned alive)
     {
-        CheckCtx<W> ctx{ev, alive, false, nullptr, nullptr};
+        CheckCtx<W, kExt> ctx{ev, alive, false, nullptr, nullptr};
         float T[12], NR[9], Nt[3];
         Robot::ee_pose(q, T);
         const float4 *A = ev.att;
@@ -154,18 +158,20 @@ namespace vg
     }
 
     // kLoopedEnv: the robot's environment section as loops (smaller code) instead of unrolled;
-    // kAttach: Robot::fkcc_attach (the environment holds an attachment)
-    template <typename Robot, int W, bool kLoopedEnv = false, bool kAttach = false>
+    // kExt: the extended checks, for environments with heightfields or an attachment: every
+    // environment query also tests the heightfields, and with an attachment the block runs
+    // Robot::fkcc_attach
+    template <typename Robot, int W, bool kLoopedEnv = false, bool kExt = false>
     __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
         static_assert(Robot::kEnvChecks <= kWarpScratch, "per-warp scratch holds one word per environment check");
         __shared__ unsigned warp_scratch[kStageStride / 32][kWarpScratch];
-        CheckCtx<W> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
-        Robot::template fkcc<CheckCtx<W>, kLoopedEnv>(q, ctx);
-        if constexpr (kAttach)
+        CheckCtx<W, kExt> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
+        Robot::template fkcc<CheckCtx<W, kExt>, kLoopedEnv>(q, ctx);
+        if constexpr (kExt)
         {
-            if (ctx.alive)
-                ctx.alive = attach_check<Robot, W>(ev, q, ctx.alive);
+            if (ctx.alive && ev.n_att >= 0)
+                ctx.alive = attach_check<Robot, W, kExt>(ev, q, ctx.alive);
         }
         return ctx.alive;
     }
@@ -180,7 +186,7 @@ namespace vg
         EnvDevice env;
     };
 
-    template <typename Robot, bool kAttach = false>
+    template <typename Robot, bool kExt = false>
     __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) states_kernel(StatesParams p)
     {
         extern __shared__ float4 smem[];
@@ -201,7 +207,7 @@ namespace vg
             {
                 q[d] = in ? p.q[idx * D + d] : 0.0f;
             }
-            const unsigned alive = run_fkcc<Robot, 1, true, kAttach>(ev, q, __ballot_sync(kFull, in), stage);
+            const unsigned alive = run_fkcc<Robot, 1, true, kExt>(ev, q, __ballot_sync(kFull, in), stage);
             if (in)
             {
                 p.out[idx] = static_cast<uint8_t>((alive >> (threadIdx.x & 31)) & 1u);
@@ -321,7 +327,7 @@ namespace vg
         return __fsqrt_rn(__fadd_rn(__fadd_rn(a0, a2), __fadd_rn(a1, a3)));
     }
 
-    template <typename Robot, int W, bool kAttach = false>
+    template <typename Robot, int W, bool kExt = false>
     __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) edges_kernel(EdgesParams p)
     {
         extern __shared__ float4 smem[];
@@ -391,7 +397,7 @@ namespace vg
             {
                 break;
             }
-            const unsigned alive = run_fkcc<Robot, W, false, kAttach>(ev, q, active, stage);
+            const unsigned alive = run_fkcc<Robot, W, false, kExt>(ev, q, active, stage);
             bool finish = false;
             if (e >= 0)
             {

@@ -6,17 +6,17 @@
 
 namespace vg
 {
-    template <typename R, bool kAttach = false>
+    template <typename R, bool kExt = false>
     cudaError_t launch_states(const StatesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        states_kernel<R, kAttach><<<grid, block, smem, s>>>(p);
+        states_kernel<R, kExt><<<grid, block, smem, s>>>(p);
         return cudaGetLastError();
     }
 
-    template <typename R, int W, bool kAttach = false>
+    template <typename R, int W, bool kExt = false>
     cudaError_t launch_edges(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
-        edges_kernel<R, W, kAttach><<<grid, block, smem, s>>>(p);
+        edges_kernel<R, W, kExt><<<grid, block, smem, s>>>(p);
         return cudaGetLastError();
     }
 
@@ -107,13 +107,13 @@ namespace vg
         o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
         o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);
         o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true>);
-        // fkcc_attach: the segment-per-edge and states kernels with the attachment checks
-        o.states_attach = &launch_states<R, true>;
-        o.states_attach_fn = reinterpret_cast<const void *>(&states_kernel<R, true>);
-        o.edges_attach[0] = &launch_edges<R, 8, true>;
-        o.edges_attach[1] = &launch_edges<R, 4, true>;
-        o.edges_attach_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8, true>);
-        o.edges_attach_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4, true>);
+        // extended checks (heightfields, fkcc_attach): the segment-per-edge and states kernels
+        o.states_ext = &launch_states<R, true>;
+        o.states_ext_fn = reinterpret_cast<const void *>(&states_kernel<R, true>);
+        o.edges_ext[0] = &launch_edges<R, 8, true>;
+        o.edges_ext[1] = &launch_edges<R, 4, true>;
+        o.edges_ext_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8, true>);
+        o.edges_ext_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4, true>);
         o.ee_pose = &launch_ee_pose<R>;
         o.stage_floats = R::kStage;
         o.spheres = &launch_spheres<R>;

@@ -927,9 +927,9 @@ def gen_cuda(model: dict) -> str:
             out.append(f"    if (need)")
             out.append("    {")
             if staged:
-                out.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, st, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
+                out.append(f"        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, st, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
             else:
-                out.append(f"        const unsigned hit = env_fine<Ctx::kW>(ctx.env, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
+                out.append(f"        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
             out.append("        if (hit && !(ctx.alive &= ~hit)) return;")
             out.append("    }")
             out.append("}")
@@ -1046,7 +1046,7 @@ for (int k = 0; k < {n_env}; ++k)
     const unsigned need = chs[k] & ctx.alive;
     if (need)
     {{
-        const unsigned hit = env_fine<Ctx::kW>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
+        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
         if (hit && !(ctx.alive &= ~hit)) return;
     }}
 }}""".split("\n")
@@ -1060,7 +1060,7 @@ for (int k = 0; k < {n_env}; ++k)
     w("#ifdef VG_FORM_COMPACT")
     w(f"""    // Fine environment tests of the spheres EnvFine[k0..k1) of one frame, for the segments in
     // `need`: the segments whose block collides.
-    template <int W>
+    template <int W, bool kExt = false>
     static __device__ __noinline__ unsigned env_fine(const vg::EnvView &ev, const vg::Frame f, int k0, int k1, unsigned need)
     {{
         unsigned dead = 0u;
@@ -1069,7 +1069,7 @@ for (int k = 0; k < {n_env}; ++k)
         {{
             const float4 o = {pre}SlotOff[{pre}EnvFine[k]];
             const float4 c = vg::frame_point(f, o);
-            const unsigned hit = vg::env_query_inline<W>(ev, c.x, c.y, c.z, c.w, need);
+            const unsigned hit = vg::env_query_inline<W, kExt>(ev, c.x, c.y, c.z, c.w, need);
             dead |= hit;
             need &= ~hit;
             if (!need)
@@ -1125,7 +1125,7 @@ for (int k = 0; k < {n_env}; ++k)
 
     // Fine environment tests of the spheres EnvFine[k0..k1) of staged frame f, for the segments
     // in `need`: the segments whose block collides.
-    template <int W>
+    template <int W, bool kExt = false>
     static __device__ __noinline__ unsigned env_fine(const vg::EnvView &ev, const float *st, int f, int k0, int k1, unsigned need)
     {{
         const vg::Frame fr = frame_at(st, f);
@@ -1135,7 +1135,7 @@ for (int k = 0; k < {n_env}; ++k)
         {{
             const float4 o = {pre}SlotOff[{pre}EnvFine[k]];
             const float4 c = vg::frame_point(fr, o);
-            const unsigned hit = vg::env_query_inline<W>(ev, c.x, c.y, c.z, c.w, need);
+            const unsigned hit = vg::env_query_inline<W, kExt>(ev, c.x, c.y, c.z, c.w, need);
             dead |= hit;
             need &= ~hit;
             if (!need)

@@ -152,6 +152,23 @@ def pointcloud_scene(seed: int, r_min: float, r_max: float, n_points: int = 50_0
     }
 
 
+def heightfield(seed: int, xd: int = 96, yd: int = 80, centre=(0.2, 0.0, -0.15), scale=(0.025, 0.03, 3.0)) -> dict:
+    """A terrain for the heightfield primitive: smooth random bumps in [0, 1] on an xd x yd grid
+    (row-major as the reference's png_to_heightfield flattens an image), placed at `centre`.  As
+    in the reference's factory, `scale` holds the cell sizes in x and y and the divisor of the
+    heights in z (height = value / scale_z + centre_z)."""
+    rng = np.random.default_rng(seed)
+    gx, gy = np.meshgrid(np.arange(xd), np.arange(yd), indexing="ij")
+    h = np.zeros((xd, yd))
+    for _ in range(12):
+        cx, cy = rng.uniform(0, xd), rng.uniform(0, yd)
+        w = rng.uniform(4, 15)
+        h += rng.uniform(0.2, 1.0) * np.exp(-((gx - cx) ** 2 + (gy - cy) ** 2) / (2 * w * w))
+    h = (h / h.max()).astype(np.float32)
+    return {"centre": np.asarray(centre, np.float32), "scale": np.asarray(scale, np.float32), "xd": xd, "yd": yd,
+            "data": h.reshape(-1)}
+
+
 def configurations(s_m, s_a, n: int, seed: int) -> np.ndarray:
     """n configurations uniform within the joint limits: q = u * s_m + s_a, u ~ U[0, 1)^dim
     (the reference's scale_configuration, robots/panda.hh:77-80)."""
