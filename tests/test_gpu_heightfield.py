@@ -56,7 +56,7 @@ def test_heightfield_checks_are_the_oracles(vg, port, robot):
     ce, cb = penv.validate_motions(prb, a, b, prb.resolution, threads=THREADS)
     assert np.array_equal(ge, ce) and np.array_equal(blocks.cpu().numpy(), cb)
     plain = rb.validate_batch(q, vg.Environment.from_scene(scenes.scene_config0(41)))
-    assert (plain & ~got).any()  # the terrain removes configurations
+    assert not (got & ~plain).any()  # the terrain only removes configurations
 
 
 def test_heightfield_pointcloud_and_attachment_together(vg, port):
