@@ -165,12 +165,15 @@ namespace vg
 
     static_assert(sizeof(CaptView) % sizeof(float4) == 0, "CaptView must pack into float4s");
 
-    // Uploads each pointcloud's tree once (4 device buffers per cloud).
+    // Uploads each pointcloud's tree once: kCloudBuffers device buffers per cloud (tests, aabbs,
+    // starts, the reference-layout blocks, the ring-ordered blocks the queries scan, and the
+    // blocks' ring bounds).  A host-built cloud's reference-layout blocks are freed once ordered
+    // (the host copy answers layout queries).
     static int upload_clouds(vg_env *e)
     {
-        while (e->d_clouds.size() < 4 * e->clouds.size())
+        while (e->d_clouds.size() < kCloudBuffers * e->clouds.size())
         {
-            const CaptHost &c = e->clouds[e->d_clouds.size() / 4];
+            const CaptHost &c = e->clouds[e->d_clouds.size() / kCloudBuffers];
             const void *src[4] = {c.tests.data(), c.aabbs.data(), c.aff_starts.data(), c.aff.data()};
             const size_t bytes[4] = {c.tests.size() * sizeof(float), c.aabbs.size() * sizeof(float),
                                      c.aff_starts.size() * sizeof(uint32_t), std::max<size_t>(16, c.aff.size() * sizeof(float))};
@@ -192,10 +195,23 @@ namespace vg
                     return cuda_fail(err, "upload pointcloud");
                 }
             }
+            float *aff_q = nullptr, *ring_lo = nullptr;
+            const int rc = capt_ring_order(static_cast<const float *>(dst[0]), c.nlog2, static_cast<const uint32_t *>(dst[2]),
+                                           static_cast<const float *>(dst[3]), c.blocks(), c.r_max, c.r_point, &aff_q, &ring_lo);
+            cudaFree(dst[3]);
+            dst[3] = nullptr;
+            if (rc != VG_OK)
+            {
+                for (int j = 0; j < 3; ++j)
+                    cudaFree(dst[j]);
+                return rc;
+            }
             for (int k = 0; k < 4; ++k)
             {
                 e->d_clouds.push_back(dst[k]);
             }
+            e->d_clouds.push_back(aff_q);
+            e->d_clouds.push_back(ring_lo);
         }
         return VG_OK;
     }
@@ -207,10 +223,12 @@ namespace vg
         {
             const CaptHost &c = e->clouds[i];
             CaptView v{};
-            v.tests = static_cast<const float *>(e->d_clouds[4 * i + 0]);
-            v.aabbs = static_cast<const float *>(e->d_clouds[4 * i + 1]);
-            v.starts = static_cast<const uint32_t *>(e->d_clouds[4 * i + 2]);
-            v.aff = static_cast<const float4 *>(e->d_clouds[4 * i + 3]);
+            void *const *d = &e->d_clouds[kCloudBuffers * i];
+            v.tests = static_cast<const float *>(d[0]);
+            v.aabbs = static_cast<const float *>(d[1]);
+            v.starts = static_cast<const uint32_t *>(d[2]);
+            v.aff = static_cast<const float4 *>(d[4]);  // ring order
+            v.ring_lo = static_cast<const float *>(d[5]);
             for (int k = 0; k < 6; ++k)
                 v.top[k] = c.top[k];
             v.r_point = c.r_point;
@@ -601,6 +619,12 @@ int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float 
     DeviceCapt d;
     if (int rc = capt_build_device(xyz, n, r_min, r_max, r_point, static_cast<cudaStream_t>(stream), d))
         return rc;
+    float *aff_q = nullptr, *ring_lo = nullptr;
+    if (int rc = capt_ring_order(d.tests, d.nlog2, d.starts, d.aff, d.blocks, r_max, r_point, &aff_q, &ring_lo))
+    {
+        d.release();
+        return rc;
+    }
     CaptHost c;
     c.nlog2 = d.nlog2;
     std::memcpy(c.top, d.top, sizeof(c.top));
@@ -613,7 +637,9 @@ int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float 
     env->d_clouds.push_back(d.tests);
     env->d_clouds.push_back(d.aabbs);
     env->d_clouds.push_back(d.starts);
-    env->d_clouds.push_back(d.aff);
+    env->d_clouds.push_back(d.aff);  // reference layout, kept for vg_env_pointcloud_layout
+    env->d_clouds.push_back(aff_q);
+    env->d_clouds.push_back(ring_lo);
     env->device = dev;
     env->dirty = true;
     return VG_OK;
@@ -632,7 +658,7 @@ int vg_env_pointcloud_layout(const vg_env *env, int index, uint64_t *sizes, floa
     if (c.on_device)
     {
         // the arrays live on the GPU that built them
-        void *const *d = &env->d_clouds[4 * static_cast<size_t>(index)];
+        void *const *d = &env->d_clouds[kCloudBuffers * static_cast<size_t>(index)];
         const size_t bytes[4] = {sizes[1] * sizeof(float), sizes[2] * 6 * sizeof(float), (sizes[2] + 1) * sizeof(uint32_t),
                                  sizes[3] * 24 * sizeof(float)};
         void *dst[4] = {tests, aabbs, aff_starts, aff};

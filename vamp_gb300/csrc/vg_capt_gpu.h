@@ -29,4 +29,11 @@ namespace vg
     // Builds the tree of n points xyz[n][3] (device memory) on the current device.
     int capt_build_device(const float *xyz, size_t n, float r_min, float r_max, float r_point, cudaStream_t s,
                           DeviceCapt &out);
+
+    // The query order of a tree's affordance lists (vg_capt_ring.cu): each leaf's points
+    // regrouped by distance to the leaf's cell, nearest ring first (aff_q, blocks x 24), and per
+    // block the lower edge of its first point's ring (ring_lo, non-decreasing within a leaf).
+    // Allocates both; synchronous.
+    int capt_ring_order(const float *tests, int nlog2, const uint32_t *starts, const float *aff, size_t blocks,
+                        float r_max, float r_point, float **aff_q, float **ring_lo);
 }  // namespace vg

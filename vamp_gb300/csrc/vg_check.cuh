@@ -179,7 +179,10 @@ namespace vg
         float r_point;
         int nlog2;
         int n_tests;
-        int pad[3];
+        int pad;
+        // per affordance block, the lower edge of the distance ring of its first point (the
+        // blocks of aff are in ring order, nearest first; vg_capt_ring.cu)
+        const float *ring_lo;
     };
     constexpr int kMaxClouds = 4;
 
@@ -420,6 +423,19 @@ namespace vg
         }
         b0 = __ldg(c.starts + leaf);
         b1 = __ldg(c.starts + leaf + 1);
+        // the leaf's blocks come nearest ring first: drop those whose ring starts beyond the
+        // sphere's reach (the margin dwarfs the FP32 error of the point test)
+        const float lim = __fmaf_rn(rad, 1e-5f, rad);
+        uint32_t lo = b0, hi = b1;
+        while (lo < hi)
+        {
+            const uint32_t mid = lo + ((hi - lo) >> 1);
+            if (__ldg(c.ring_lo + mid) > lim)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        b1 = lo;
     }
 
     // Whether any of the 8 points of affordance block b lies within sqrt(rc) of (x, y, z).

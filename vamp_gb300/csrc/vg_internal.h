@@ -67,6 +67,10 @@ namespace vg
         }                                   \
     } while (0)
 
+    // device buffers per pointcloud: tests, aabbs, starts, reference-layout blocks (device-built
+    // clouds only), ring-ordered blocks, ring bounds
+    constexpr size_t kCloudBuffers = 6;
+
     // threads per block of every checking kernel (the robots' stage stride)
     constexpr int kBlock = 128;
     static_assert(kBlock == kStageStride, "stage columns are one per thread of a block");
@@ -113,7 +117,7 @@ struct vg_env
     int n[5] = {0, 0, 0, 0, 0};
     // pointclouds: host trees and their device copies (tests, aabbs, starts, aff per cloud)
     std::vector<vg::CaptHost> clouds;
-    std::vector<void *> d_clouds;  // 4 buffers per uploaded cloud
+    std::vector<void *> d_clouds;  // kCloudBuffers buffers per uploaded cloud
     // library-owned scratch: work counter, staging for host-pointer calls
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;
