@@ -375,6 +375,15 @@ def run_filter(args, world, rank, local):
         vg.Environment().add_pointcloud_device(kept, m["min_radius"], m["max_radius"], scenes.POINT_RADIUS)
         ts.append(t1 - t0)
         tb.append(time.perf_counter() - t1)
+    # the same cloud without the cull: every point takes part in all six passes
+    for _ in range(2):
+        vg.filter_pointcloud_device(d_pts, md, rad, org, org - rad, org + rad, False)
+    tn = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kept_all = vg.filter_pointcloud_device(d_pts, md, rad, org, org - rad, org + rad, False)
+        tn.append(time.perf_counter() - t0)
     host, ns = vg.filter_pointcloud(pts, md, rad, org, org - rad, org + rad, True)
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -390,6 +399,8 @@ def run_filter(args, world, rank, local):
             "metric": "pointcloud filter on 1 GB300 (filter_pointcloud)", "value": len(pts) / (ms / 1e3),
             "unit": "points/s", "ms_per_step": ms, "points": len(pts), "kept": int(kept.shape[0]),
             "capt_build_gpu_ms": 1e3 * float(np.median(tb)), "host_buffers_ms": ns / 1e6,
+            "no_cull": {"ms": 1e3 * float(np.median(tn)), "points_per_s": len(pts) / float(np.median(tn)),
+                        "kept": int(kept_all.shape[0])},
             "cpu_baseline": None if cpu is None else {"value": len(pts) / cpu, "unit": "points/s", "cores": 1,
                                                       "kind": "port", "sample": "the whole cloud, once"},
             "steps": args.steps, "warmup": args.warmup,

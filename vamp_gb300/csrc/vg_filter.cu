@@ -495,39 +495,51 @@ namespace vg
             }
         }
 
-        // kept flags of each chunk: its chain members from the entry point
+        // kept flags of each chunk: its chain members from the entry point.  Each thread lifts
+        // from the entry with the doubling tables J_k = next^(2^k) (restricted to the chunk):
+        // the last chain element at or before its own index is itself exactly when it is kept.
         __global__ void mark_kept(const uint32_t *next, long long m, const uint32_t *entry, uint32_t *kept, uint32_t *err)
         {
-            __shared__ uint32_t nx[kTile], flag[kTile];
+            __shared__ uint32_t J[10][kTile];
             const long long c0 = static_cast<long long>(blockIdx.x) * kTile;
             const long long c1 = c0 + kTile < m ? c0 + kTile : m;
             const int t = threadIdx.x;
-            nx[t] = c0 + t < c1 ? next[c0 + t] : static_cast<uint32_t>(c1);
-            flag[t] = 0;
-            __syncthreads();
-            if (t == 0)
+            const uint32_t e0 = entry[blockIdx.x];
+            if (e0 == 0xFFFFFFFFu)
             {
-                const uint32_t e0 = entry[blockIdx.x];
-                if (e0 != 0xFFFFFFFFu)
-                {
-                    if (e0 < c0)
-                        *err = 2u;  // not reached: the walk records entries inside their chunk
-                    for (long long e = e0; e >= c0 && e < c1;)
-                    {
-                        flag[e - c0] = 1;
-                        const long long x = nx[e - c0];
-                        if (x <= e)
-                        {
-                            *err = 3u;  // not reached: next[j] > j
-                            break;
-                        }
-                        e = x;
-                    }
-                }
+                if (c0 + t < c1)
+                    kept[c0 + t] = 0u;
+                return;  // uniform: the chain skips this chunk
             }
+            J[0][t] = c0 + t < c1 ? next[c0 + t] : static_cast<uint32_t>(c1);
             __syncthreads();
+            for (int k = 1; k < 10; ++k)
+            {
+                const uint32_t v = J[k - 1][t];
+                J[k][t] = v < c1 && v > c0 ? J[k - 1][v - c0] : v;
+                __syncthreads();
+            }
             if (c0 + t < c1)
-                kept[c0 + t] = flag[t];
+            {
+                uint32_t mine = 0u;
+                const uint32_t me = static_cast<uint32_t>(c0 + t);
+                if (e0 < c0 || e0 >= c1)
+                {
+                    *err = 2u;  // not reached: the walk records entries inside their chunk
+                }
+                else if (e0 <= me)
+                {
+                    uint32_t cur = e0;
+                    for (int k = 9; k >= 0; --k)
+                    {
+                        const uint32_t v = J[k][cur - c0];
+                        if (v <= me)
+                            cur = v;
+                    }
+                    mine = cur == me ? 1u : 0u;
+                }
+                kept[c0 + t] = mine;
+            }
         }
 
         __global__ void gather_points(const float *xyz, const uint32_t *list, long long m, float *out)
