@@ -330,6 +330,8 @@ namespace vg
         {
             d.field.g_lo[k] = e->field.g_lo[k];
             d.field.dim[k] = e->field.dim[k];
+            d.field.p_lo[k] = e->field.p_lo[k];
+            d.field.p_hi[k] = e->field.p_hi[k];
         }
         d.field.inv_cell = e->field.inv_cell;
         return d;

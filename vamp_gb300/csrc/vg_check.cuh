@@ -207,6 +207,7 @@ namespace vg
         float g_lo[3];
         float inv_cell;
         int dim[3];
+        float p_lo[3], p_hi[3];  // the primitives' bounding box
     };
 
     struct EnvView
@@ -224,19 +225,37 @@ namespace vg
         FieldView field;
     };
 
-    // Whether no primitive test can be negative for the sphere (x, y, z, r): its centre lies in
-    // the field's grid and the cell's bound exceeds r + 1e-4 m, far above the FP32 error of the
-    // tests.  Centres outside the grid (or NaN) answer false.  The field must exist.
+    // Whether no primitive test can be negative for the sphere (x, y, z, r): its centre's cell
+    // bound (or, outside the grid, its distance to the primitives' box) exceeds r + 1e-4 m, far
+    // above the FP32 error of the tests.  NaN coordinates answer false.
     __device__ __forceinline__ bool field_far(const FieldView &f, float x, float y, float z, float r)
     {
-        const int i = __float2int_rd(__fmul_rn(__fsub_rn(x, f.g_lo[0]), f.inv_cell));
-        const int j = __float2int_rd(__fmul_rn(__fsub_rn(y, f.g_lo[1]), f.inv_cell));
-        const int k = __float2int_rd(__fmul_rn(__fsub_rn(z, f.g_lo[2]), f.inv_cell));
-        const bool in = static_cast<unsigned>(i) < static_cast<unsigned>(f.dim[0]) &&
-                        static_cast<unsigned>(j) < static_cast<unsigned>(f.dim[1]) &&
-                        static_cast<unsigned>(k) < static_cast<unsigned>(f.dim[2]);
-        const float lb = __ldg(f.data + (in ? (k * f.dim[1] + j) * f.dim[0] + i : 0));
-        return in && lb > __fadd_rn(r, 1e-4f);
+        if (!f.data)
+        {
+            return false;
+        }
+        const float lim = __fadd_rn(r, 1e-4f);
+        const float fx = __fmul_rn(__fsub_rn(x, f.g_lo[0]), f.inv_cell);
+        const float fy = __fmul_rn(__fsub_rn(y, f.g_lo[1]), f.inv_cell);
+        const float fz = __fmul_rn(__fsub_rn(z, f.g_lo[2]), f.inv_cell);
+        if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < static_cast<float>(f.dim[0]) &&
+            fy < static_cast<float>(f.dim[1]) && fz < static_cast<float>(f.dim[2]))
+        {
+            const int i = min(static_cast<int>(fx), f.dim[0] - 1), j = min(static_cast<int>(fy), f.dim[1] - 1),
+                      k = min(static_cast<int>(fz), f.dim[2] - 1);
+            return __ldg(f.data + (static_cast<long long>(k) * f.dim[1] + j) * f.dim[0] + i) > lim;
+        }
+        const float p[3] = {x, y, z};
+        float d2 = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            const float below = __fsub_rn(f.p_lo[a], p[a]), above = __fsub_rn(p[a], f.p_hi[a]);
+            const float d = below > above ? below : above;
+            const float dd = d > 0.0f ? d : 0.0f;
+            d2 = __fmaf_rn(dd, dd, d2);
+        }
+        return d2 > __fmul_rn(__fmul_rn(lim, lim), 1.00001f);
     }
 
     // sphere_heightfield (collision/sphere_heightfield.hh:9-30), sign bit set iff the sphere is
@@ -553,11 +572,8 @@ namespace vg
     // sphere s.  Warp-uniform; all 32 lanes must call.
     // kExt: also the heightfields (kernels built for environments with heightfields or an
     // attachment; the default kernels leave them out)
-    // skip: spheres (bit s) the clearance field puts out of every primitive's reach for every
-    // lane of the warp (CheckCtx::field_skip): their primitive passes are left out
     template <int W, int NS, bool kExt = false>
-    __device__ __forceinline__ void env_multi(const EnvView &e, const float4 *sph, unsigned mask, unsigned *hit,
-                                              unsigned skip = 0u)
+    __device__ __forceinline__ void env_multi(const EnvView &e, const float4 *sph, unsigned mask, unsigned *hit)
     {
         const int lane = threadIdx.x & 31;
         const bool on = (mask >> lane) & 1u;
@@ -574,15 +590,20 @@ namespace vg
             r[s] = c.w;
             rsq[s] = __fmul_rn(c.w, c.w);
             bits[s] = 0u;
+            // a sphere no lane of the warp brings within reach of a primitive skips the primitive
+            // passes (its OR over their tests is false)
+            if (!__any_sync(kFull, on && !field_far(e.field, c.x, c.y, c.z, c.w)))
+            {
+                M[s] = -__int_as_float(0x7f800000);
+                Mw[s] = -__int_as_float(0x7f800000);
+                continue;
+            }
             const float v = __fmaf_rn(c.x, c.x, __fmaf_rn(c.z, c.z, __fmul_rn(c.y, c.y)));
             const float m = seg_max<W>(max_extent(e, v, c.w));
-            // a sphere no lane of the warp brings within reach of a primitive (skip) counts as
-            // inactive in every lane: its OR over the primitive tests is false
-            const bool live = on && !((skip >> s) & 1u);
-            M[s] = live ? m : -__int_as_float(0x7f800000);
+            M[s] = on ? m : -__int_as_float(0x7f800000);
             // max_extent is >= 0 (or +inf): as unsigned integers its bit patterns order like the
             // floats, so one warp reduction gives the warp-wide bound (inactive lanes count as 0)
-            Mw[s] = __uint_as_float(__reduce_max_sync(kFull, live ? __float_as_uint(m) : 0u));
+            Mw[s] = __uint_as_float(__reduce_max_sync(kFull, on ? __float_as_uint(m) : 0u));
             Mall = fmaxf(Mall, Mw[s]);
         }
         kind_pass<0, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
@@ -726,35 +747,10 @@ namespace vg
             return env_query<W, kExt>(env, x, y, z, r, mask);
         }
 
-        // the spheres s[0..N) (bit k) that the clearance field puts out of every primitive's
-        // reach for every lane of `alive`; all N lookups are issued together
-        template <int N>
-        __device__ __forceinline__ unsigned field_skip(const float4 *s)
-        {
-            if (!env.field.data)
-            {
-                return 0u;
-            }
-            const bool on = (alive >> (threadIdx.x & 31)) & 1u;
-            bool far[N];
-#pragma unroll
-            for (int k = 0; k < N; ++k)
-            {
-                far[k] = field_far(env.field, s[k].x, s[k].y, s[k].z, s[k].w);
-            }
-            unsigned bits = 0u;
-#pragma unroll
-            for (int k = 0; k < N; ++k)
-            {
-                bits |= __all_sync(kFull, !on || far[k]) ? 1u << k : 0u;
-            }
-            return bits;
-        }
-
         template <int NS>
-        __device__ __forceinline__ void env_many(const float4 *s, unsigned mask, unsigned *hit, unsigned skip = 0u)
+        __device__ __forceinline__ void env_many(const float4 *s, unsigned mask, unsigned *hit)
         {
-            env_multi<W, NS, kExt>(env, s, mask, hit, skip);
+            env_multi<W, NS, kExt>(env, s, mask, hit);
         }
 
         template <int NS>

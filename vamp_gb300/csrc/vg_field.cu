@@ -1,5 +1,5 @@
 // Clearance field of an environment's primitives: a grid over their bounding box (widened by
-// 30 cm, so that robot spheres near the scene fall inside it) whose cells hold a lower bound of the distance from any point of the cell to the
+// 10 cm) whose cells hold a lower bound of the distance from any point of the cell to the
 // nearest primitive, as each primitive's collision test measures it:
 //   sphere       |x - c| - R
 //   capsule      distance to the segment - R (the test's clamped projection is some point of
@@ -185,8 +185,8 @@ namespace vg
             if (!std::isfinite(lo[k]) || !std::isfinite(hi[k]) || hi[k] - lo[k] > 1e6)
                 return VG_OK;  // no usable box: queries go without the field
         }
-        constexpr double kWiden = 0.3, kMinCell = 0.025;
-        constexpr int kMaxDim = 160;
+        constexpr double kWiden = 0.1, kMinCell = 0.02;
+        constexpr int kMaxDim = 200;
         FieldGeom g{};
         double span = 0.0;
         for (int k = 0; k < 3; ++k)
@@ -219,8 +219,11 @@ namespace vg
         }
         for (int k = 0; k < 3; ++k)
         {
+            // the grid's corner and the primitives' box, rounded outwards to FP32
             out.g_lo[k] = static_cast<float>(g.lo[k]);
             out.dim[k] = g.dim[k];
+            out.p_lo[k] = std::nextafter(static_cast<float>(lo[k]), -INFINITY);
+            out.p_hi[k] = std::nextafter(static_cast<float>(hi[k]), INFINITY);
         }
         out.inv_cell = static_cast<float>(1.0 / g.cell);
         out.cell = static_cast<float>(g.cell);

@@ -74,6 +74,7 @@ namespace vg
         float g_lo[3] = {0, 0, 0};
         float inv_cell = 0, cell = 0;
         int dim[3] = {0, 0, 0};
+        float p_lo[3] = {0, 0, 0}, p_hi[3] = {0, 0, 0};  // the primitives' bounding box
         void release();
     };
 

@@ -902,12 +902,11 @@ def gen_cuda(model: dict) -> str:
         coarse.append(f"    cs[{k}] = make_float4({x}, {y}, {z}, {r});  // {e['link']}")
         coarse.append("}")
     coarse.append(f"unsigned ch[{n_env}];")
-    coarse.append(f"const unsigned far = ctx.template field_skip<{n_env}>(cs);  // out of every primitive's reach")
     nb = -(-n_env // COARSE_BATCH)
     base = 0
     for bi in range(nb):
         size = n_env // nb + (1 if bi < n_env % nb else 0)
-        coarse.append(f"ctx.template env_many<{size}>(cs + {base}, ctx.alive, ch + {base}, far >> {base});")
+        coarse.append(f"ctx.template env_many<{size}>(cs + {base}, ctx.alive, ch + {base});")
         base += size
 
     stage = []
@@ -1029,7 +1028,7 @@ for (int b = 0; b < {nb}; ++b)
                             : make_float4(1.0e10f, 0.0f, 0.0f, -__int_as_float(0x7f800000));
     }}
     unsigned h[4];
-    ctx.template env_many<4>(sp, ctx.alive, h, ctx.template field_skip<4>(sp));
+    ctx.template env_many<4>(sp, ctx.alive, h);
 #pragma unroll
     for (int s = 0; s < 4; ++s)
     {{
