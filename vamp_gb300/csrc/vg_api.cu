@@ -264,8 +264,6 @@ namespace vg
             e->d_hf.push_back(p);
             VG_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice), "upload heightfield");
         }
-        if (int rc = build_field(e, e->field))
-            return rc;
         std::vector<float4> img;
         pack_image(e, img, e->off, e->n);
         pack_clouds(e, img, &e->cloud_off);
@@ -325,15 +323,6 @@ namespace vg
         d.att_off = e->att_off;
         d.n_hf = static_cast<int>(e->hf.size());
         d.hf_off = e->hf_off;
-        d.field.data = e->field.data;
-        for (int k = 0; k < 3; ++k)
-        {
-            d.field.g_lo[k] = e->field.g_lo[k];
-            d.field.dim[k] = e->field.dim[k];
-            d.field.p_lo[k] = e->field.p_lo[k];
-            d.field.p_hi[k] = e->field.p_hi[k];
-        }
-        d.field.inv_cell = e->field.inv_cell;
         return d;
     }
 
@@ -549,7 +538,6 @@ void vg_env_destroy(vg_env *env)
         cudaFree(p);
     for (void *p : env->d_hf)
         cudaFree(p);
-    env->field.release();
     delete env;
 }
 

@@ -199,17 +199,6 @@ namespace vg
     };
     constexpr int kMaxHeightfields = 8;
 
-    // Clearance field of the primitives (built by vg_field.cu): per grid cell a lower bound of
-    // the distance from any point of the cell to the nearest primitive, as the tests measure it.
-    struct FieldView
-    {
-        const float *data;  // null: no field
-        float g_lo[3];
-        float inv_cell;
-        int dim[3];
-        float p_lo[3], p_hi[3];  // the primitives' bounding box
-    };
-
     struct EnvView
     {
         const float4 *rec[5];
@@ -222,41 +211,7 @@ namespace vg
         int n_att;          // -1: none
         const HeightView *hf;
         int n_hf;
-        FieldView field;
     };
-
-    // Whether no primitive test can be negative for the sphere (x, y, z, r): its centre's cell
-    // bound (or, outside the grid, its distance to the primitives' box) exceeds r + 1e-4 m, far
-    // above the FP32 error of the tests.  NaN coordinates answer false.
-    __device__ __forceinline__ bool field_far(const FieldView &f, float x, float y, float z, float r)
-    {
-        if (!f.data)
-        {
-            return false;
-        }
-        const float lim = __fadd_rn(r, 1e-4f);
-        const float fx = __fmul_rn(__fsub_rn(x, f.g_lo[0]), f.inv_cell);
-        const float fy = __fmul_rn(__fsub_rn(y, f.g_lo[1]), f.inv_cell);
-        const float fz = __fmul_rn(__fsub_rn(z, f.g_lo[2]), f.inv_cell);
-        if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < static_cast<float>(f.dim[0]) &&
-            fy < static_cast<float>(f.dim[1]) && fz < static_cast<float>(f.dim[2]))
-        {
-            const int i = min(static_cast<int>(fx), f.dim[0] - 1), j = min(static_cast<int>(fy), f.dim[1] - 1),
-                      k = min(static_cast<int>(fz), f.dim[2] - 1);
-            return __ldg(f.data + (static_cast<long long>(k) * f.dim[1] + j) * f.dim[0] + i) > lim;
-        }
-        const float p[3] = {x, y, z};
-        float d2 = 0.0f;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-        {
-            const float below = __fsub_rn(f.p_lo[a], p[a]), above = __fsub_rn(p[a], f.p_hi[a]);
-            const float d = below > above ? below : above;
-            const float dd = d > 0.0f ? d : 0.0f;
-            d2 = __fmaf_rn(dd, dd, d2);
-        }
-        return d2 > __fmul_rn(__fmul_rn(lim, lim), 1.00001f);
-    }
 
     // sphere_heightfield (collision/sphere_heightfield.hh:9-30), sign bit set iff the sphere is
     // below the surface: the cell floor(clamp(xs * (x0 - x) + xd / 2, 0, xd)) (one fused
@@ -589,15 +544,6 @@ namespace vg
             z[s] = c.z;
             r[s] = c.w;
             rsq[s] = __fmul_rn(c.w, c.w);
-            bits[s] = 0u;
-            // a sphere no lane of the warp brings within reach of a primitive skips the primitive
-            // passes (its OR over their tests is false)
-            if (!__any_sync(kFull, on && !field_far(e.field, c.x, c.y, c.z, c.w)))
-            {
-                M[s] = -__int_as_float(0x7f800000);
-                Mw[s] = -__int_as_float(0x7f800000);
-                continue;
-            }
             const float v = __fmaf_rn(c.x, c.x, __fmaf_rn(c.z, c.z, __fmul_rn(c.y, c.y)));
             const float m = seg_max<W>(max_extent(e, v, c.w));
             M[s] = on ? m : -__int_as_float(0x7f800000);
@@ -605,6 +551,7 @@ namespace vg
             // floats, so one warp reduction gives the warp-wide bound (inactive lanes count as 0)
             Mw[s] = __uint_as_float(__reduce_max_sync(kFull, on ? __float_as_uint(m) : 0u));
             Mall = fmaxf(Mall, Mw[s]);
+            bits[s] = 0u;
         }
         kind_pass<0, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);
         kind_pass<1, NS>(e, Mall, Mw, M, x, y, z, r, rsq, bits);

@@ -60,7 +60,6 @@ namespace vg
         ev.sqrt_mode = p.env.sqrt_mode;
         ev.clouds = nullptr;
         ev.n_clouds = 0;
-        ev.field.data = nullptr;  // the reports test every object up to the stop
         for (int k = 0; k < 5; ++k)
         {
             ev.rec[k] = p.env.buf + p.env.off[k];

@@ -67,17 +67,6 @@ namespace vg
         }                                   \
     } while (0)
 
-    // Clearance field of the primitives (vg_field.cu): a grid of distance lower bounds.
-    struct EnvField
-    {
-        float *data = nullptr;  // dim[0] x dim[1] x dim[2] cells, x fastest; null: no field
-        float g_lo[3] = {0, 0, 0};
-        float inv_cell = 0, cell = 0;
-        int dim[3] = {0, 0, 0};
-        float p_lo[3] = {0, 0, 0}, p_hi[3] = {0, 0, 0};  // the primitives' bounding box
-        void release();
-    };
-
     // device buffers per pointcloud: tests, aabbs, starts, reference-layout blocks (device-built
     // clouds only), ring-ordered blocks, ring bounds
     constexpr size_t kCloudBuffers = 6;
@@ -123,8 +112,6 @@ struct vg_env
     std::vector<std::vector<float>> hf_data;
     std::vector<void *> d_hf;
     int hf_off = 0;
-    // clearance field of the primitives, rebuilt with every upload of the image
-    vg::EnvField field;
     // environments with heightfields or an attachment run the extended kernels
     bool extended() const { return n_att >= 0 || !hf.empty(); }
     int n[5] = {0, 0, 0, 0, 0};
@@ -163,8 +150,6 @@ namespace vg
     };
 
     int commit(vg_env *e);
-    // (re)builds e's clearance field from its primitives (vg_field.cu)
-    int build_field(const vg_env *e, EnvField &out);
     EnvDevice env_device(const vg_env *e);
     int sm_count();
     int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm);

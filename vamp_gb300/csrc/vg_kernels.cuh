@@ -46,7 +46,6 @@ namespace vg
         int att_off;        // attachment block: 3 transform rows, then the spheres, in float4
         int n_hf;           // HeightView descriptors
         int hf_off;         // their offset, in float4
-        FieldView field;    // clearance field of the primitives (field.data null: none)
     };
 
     constexpr int kRsqrtF4 = 2048 / 4;
@@ -76,7 +75,6 @@ namespace vg
         v.n_att = d.n_att;
         v.hf = reinterpret_cast<const HeightView *>(smem + d.hf_off - kRsqrtF4);
         v.n_hf = d.n_hf;
-        v.field = d.field;
         for (int k = 0; k < 5; ++k)
         {
             v.rec[k] = smem + d.off[k] - kRsqrtF4;
