@@ -407,6 +407,37 @@ def run_filter(args, world, rank, local):
             "timing": "wall clock of the synchronous device call (allocation included)"}))
 
 
+def run_roadmap(args, world, rank, local):
+    """Batched roadmap (vamp_gb300.roadmap): 16,384 Panda samples in the 60-primitive scene; the
+    valid ones joined to their PRM* neighbours among the earlier ones, every candidate edge
+    checked in one batch at resolution 32.  Wall clock of the whole build (synchronous)."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300.roadmap import build_roadmap
+
+    torch.cuda.set_device(local)
+    env = vg.Environment.from_scene(scenes.scene_config1(SCENE_SEED))
+    q = torch.from_numpy(scenes.configurations(vg.panda.s_m, vg.panda.s_a, 16384, 61)).cuda()
+    for _ in range(max(args.warmup, 3)):
+        rm = build_roadmap(vg.panda, env, q)
+    ts = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rm = build_roadmap(vg.panda, env, q)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.median(ts))
+    if rank == 0:
+        print(json.dumps({"metric": "batched roadmap build on 1 GB300 (PRM* neighbour edges in one batch)",
+                          "ms_per_step": ms, "samples": len(q), "nodes": rm["valid_samples"],
+                          "candidate_edges": rm["candidates"], "valid_edges": rm["valid_edges"],
+                          "candidate_edges_per_s": rm["candidates"] / (ms / 1e3), "steps": args.steps,
+                          "warmup": args.warmup, "timing": "wall clock of the synchronous build"}))
+
+
 MIXED_ROBOTS = ("ur5", "fetch", "baxter", "panda")
 MIXED_EDGES = 16384
 
@@ -762,10 +793,10 @@ def main():
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
                          "2 warp per edge with the register-rich build")
-    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug", "filter"],
+    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug", "filter", "roadmap"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
                          "mixed: four robots in one CUDA graph; debug: per-sphere collision reports; "
-                         "filter: the pointcloud filter and CAPT build")
+                         "filter: the pointcloud filter and CAPT build; roadmap: a batched PRM* roadmap")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
@@ -778,6 +809,8 @@ def main():
         run_debug(args, world, rank, local)
     elif args.workload == "filter":
         run_filter(args, world, rank, local)
+    elif args.workload == "roadmap":
+        run_roadmap(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:
