@@ -144,6 +144,16 @@ int vg_env_get(const vg_env *env, int kind, size_t index, float *out);
  * (bindings/robot_helper.hh:256-267; robots/panda.hh:5227 fkcc). */
 int vg_validate_states_device(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out, void *stream);
 
+/* planning::validate_vector<Robot, lanes, resolution> (planning/validate.hh:23-63), as the
+ * reference's planners call it (rrtc.hh:136,176; aorrtc.hh:191,227,280): edge e starts at
+ * start[e][dim], moves by vector[e][dim], and is checked in max(ceil(distance[e] / lanes *
+ * resolution), 1) blocks, distance[e] being the length the caller gives.  _device: device
+ * pointers, stream-ordered, optional blocks[n]; host form: host buffers, synchronous. */
+int vg_validate_vectors_device(const char *robot, vg_env *env, const float *start, const float *vector,
+                               const float *distance, size_t n, int resolution, uint8_t *out, int32_t *blocks,
+                               void *stream);
+int vg_validate_vectors(const char *robot, vg_env *env, const float *start, const float *vector, const float *distance,
+                        size_t n, int resolution, uint8_t *out);
 /* Per-edge validity of the straight-line motions a[i] -> b[i]: out[i] = 1 if valid.
  * Replaces planning::validate_motion<Robot, lanes, resolution> (planning/validate.hh:24-77).
  * blocks (optional, may be NULL) receives the number of lane-blocks checked per edge. */

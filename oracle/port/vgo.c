@@ -688,14 +688,13 @@ long vgo_motion_block_count(const vgo_robot *r, int lanes, const float *a, const
  * resolution), 1) blocks in total; every further block steps all lanes back by v / (lanes * n) by
  * repeated subtraction, so the edge's 8n states are visited coarse to fine.  The start state is
  * never checked.  The first invalid block ends the check. */
-static int motion(const vgo_robot *r, const vgo_env *e, int lanes, const float *a, const float *b, int resolution,
-                  int *blocks, float *rec, size_t cap, long *nrec)
+/* validate_vector (planning/validate.hh:23-63): start a, vector v, the block count from len */
+static int vector_check(const vgo_robot *r, const vgo_env *e, int lanes, const float *a, const float *v, float len,
+                        int resolution, int *blocks, float *rec, size_t cap, long *nrec)
 {
     const int dim = r->dim;
-    float v[VGO_MAX_DIM], q[VGO_MAX_LANES * VGO_MAX_DIM], bs[VGO_MAX_DIM];
-    for (int d = 0; d < dim; ++d)
-        v[d] = b[d] - a[d];
-    const long n = block_count(lanes, edge_length(dim, v), resolution);
+    float q[VGO_MAX_LANES * VGO_MAX_DIM], bs[VGO_MAX_DIM];
+    const long n = block_count(lanes, len, resolution);
     for (int l = 0; l < lanes; ++l)
     {
         const float pct = (float)(l + 1) / (float)lanes;
@@ -731,10 +730,26 @@ static int motion(const vgo_robot *r, const vgo_env *e, int lanes, const float *
     return valid;
 }
 
+/* validate_motion (planning/validate.hh:65-77): the vector b - a and its length */
+static int motion(const vgo_robot *r, const vgo_env *e, int lanes, const float *a, const float *b, int resolution,
+                  int *blocks, float *rec, size_t cap, long *nrec)
+{
+    float v[VGO_MAX_DIM];
+    for (int d = 0; d < r->dim; ++d)
+        v[d] = b[d] - a[d];
+    return vector_check(r, e, lanes, a, v, edge_length(r->dim, v), resolution, blocks, rec, cap, nrec);
+}
+
 int vgo_validate_motion(
     const vgo_robot *r, const vgo_env *e, int lanes, const float *a, const float *b, int resolution, int *blocks)
 {
     return motion(r, e, lanes, a, b, resolution, blocks, NULL, 0, NULL);
+}
+
+int vgo_validate_vector(const vgo_robot *r, const vgo_env *e, int lanes, const float *start, const float *vector,
+                        float distance, int resolution, int *blocks)
+{
+    return vector_check(r, e, lanes, start, vector, distance, resolution, blocks, NULL, 0, NULL);
 }
 
 long vgo_motion_blocks(const vgo_robot *r, int lanes, const float *a, const float *b, int resolution, float *out, size_t cap)
@@ -752,6 +767,7 @@ typedef struct
     const vgo_env *e;
     int lanes, resolution, mode; /* mode 0: states, 1: motions */
     const float *a, *b;
+    const float *dist; /* mode 2 (vectors): the lengths */
     uint8_t *out;
     int32_t *blocks;
     size_t n;
@@ -783,8 +799,10 @@ static void *worker(void *arg)
             else
             {
                 int nb = 0;
-                j->out[i] = (uint8_t)vgo_validate_motion(
-                    j->r, j->e, j->lanes, j->a + i * dim, j->b + i * dim, j->resolution, &nb);
+                j->out[i] = (uint8_t)(j->mode == 2 ? vgo_validate_vector(j->r, j->e, j->lanes, j->a + i * dim,
+                                                                          j->b + i * dim, j->dist[i], j->resolution, &nb)
+                                                   : vgo_validate_motion(j->r, j->e, j->lanes, j->a + i * dim,
+                                                                         j->b + i * dim, j->resolution, &nb));
                 if (j->blocks)
                     j->blocks[i] = nb;
             }
@@ -847,6 +865,25 @@ void vgo_validate_motions(
     j.resolution = resolution;
     j.a = a;
     j.b = b;
+    j.out = out;
+    j.blocks = blocks;
+    j.n = n;
+    run_job(&j, nthreads);
+}
+
+void vgo_validate_vectors(const vgo_robot *r, const vgo_env *e, int lanes, const float *start, const float *vector,
+                          const float *distance, size_t n, int resolution, uint8_t *out, int32_t *blocks, int nthreads)
+{
+    job_t j;
+    memset(&j, 0, sizeof(j));
+    j.r = r;
+    j.e = e;
+    j.mode = 2;
+    j.lanes = lanes;
+    j.resolution = resolution;
+    j.a = start;
+    j.b = vector;
+    j.dist = distance;
     j.out = out;
     j.blocks = blocks;
     j.n = n;

@@ -79,6 +79,13 @@ int vgo_fkcc(const vgo_robot *r, const vgo_env *e, int lanes, const float *q);
  * *blocks receives the number of fkcc calls made (may be NULL). */
 int vgo_validate_motion(
     const vgo_robot *r, const vgo_env *e, int lanes, const float *a, const float *b, int resolution, int *blocks);
+/* validate_vector<Robot, lanes, resolution> (planning/validate.hh:23-63): start, vector, and the
+ * length that sets the block count.  Returns 1 if valid; *blocks as for vgo_validate_motion. */
+int vgo_validate_vector(const vgo_robot *r, const vgo_env *e, int lanes, const float *start, const float *vector,
+                        float distance, int resolution, int *blocks);
+/* a batch of validate_vector on nthreads host threads (start, vector [n][dim], distance [n]) */
+void vgo_validate_vectors(const vgo_robot *r, const vgo_env *e, int lanes, const float *start, const float *vector,
+                          const float *distance, size_t n, int resolution, uint8_t *out, int32_t *blocks, int nthreads);
 /* states visited by validate_motion, in visiting order: up to cap blocks of [lanes][dim] */
 long vgo_motion_blocks(const vgo_robot *r, int lanes, const float *a, const float *b, int resolution, float *out, size_t cap);
 /* number of blocks validate_motion would check if no block collides: max(ceil(L / lanes * res), 1) */

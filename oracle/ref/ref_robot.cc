@@ -107,6 +107,29 @@ namespace
         }
     }
 
+    template <typename R>
+    inline bool vector_motion(const float *a, const float *v, float distance, int resolution,
+                              const collision::Environment<FloatVector<kRake>> &env)
+    {
+        const auto s = to_config(a);
+        const auto w = to_config(v);
+        switch (resolution)
+        {
+            case 1:
+                return planning::validate_vector<R, kRake, 1>(s, w, distance, env);
+            case 8:
+                return planning::validate_vector<R, kRake, 8>(s, w, distance, env);
+            case 16:
+                return planning::validate_vector<R, kRake, 16>(s, w, distance, env);
+            case 32:
+                return planning::validate_vector<R, kRake, 32>(s, w, distance, env);
+            case 64:
+                return planning::validate_vector<R, kRake, 64>(s, w, distance, env);
+            default:
+                return false;
+        }
+    }
+
     template <typename F>
     void parallel_for(std::size_t n, int nthreads, F &&f)
     {
@@ -258,6 +281,33 @@ void VG_FN(_validate_motions)(
         [&](std::size_t i)
         {
             out[i] = motion<Robot>(a + i * Robot::dimension, b + i * Robot::dimension, resolution, ev) ? 1 : 0;
+        });
+}
+
+// validate_vector<Robot, lanes, resolution> (planning/validate.hh:23-63) for a batch: start and
+// vector [n][dim], distance [n].
+void VG_FN(_validate_vectors)(
+    void *env,
+    const float *start,
+    const float *vector,
+    const float *distance,
+    std::size_t n,
+    int resolution,
+    uint8_t *out,
+    int nthreads)
+{
+    auto *e = static_cast<RefEnv *>(env);
+    e->finalize();
+    const auto &ev = *e->vec;
+    parallel_for(
+        n,
+        nthreads,
+        [&](std::size_t i)
+        {
+            out[i] = vector_motion<Robot>(start + i * Robot::dimension, vector + i * Robot::dimension, distance[i],
+                                          resolution, ev) ?
+                         1 :
+                         0;
         });
 }
 

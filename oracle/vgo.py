@@ -141,6 +141,7 @@ class Port:
         lib.vgo_robot_self_pairs.argtypes = [_p]
         lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
         lib.vgo_env_add_heightfield.argtypes = [_p, _p, _p, ctypes.c_int, ctypes.c_int, _p]
+        lib.vgo_validate_vectors.argtypes = [_p, _p, ctypes.c_int, _p, _p, _p, _sz, ctypes.c_int, _p, _p, ctypes.c_int]
         lib.vgo_env_attach.argtypes = [_p, _p, _p, ctypes.c_int]
         lib.vgo_env_detach.argtypes = [_p]
         lib.vgo_robot_ee_pose.argtypes = [_p, _p, _p]
@@ -302,6 +303,18 @@ class PortEnv:
         q = np.ascontiguousarray(q, np.float32)
         return self.port.lib.vgo_fkcc(robot.h, self.h, q.shape[0], _ptr(q))
 
+    def validate_vectors(self, robot: PortRobot, start, vector, distance, resolution: int, lanes: int = 8,
+                         threads: int = 1):
+        """validate_vector (planning/validate.hh:23-63) per edge: (verdicts, blocks checked)."""
+        s = np.ascontiguousarray(start, np.float32)
+        v = np.ascontiguousarray(vector, np.float32)
+        d = np.ascontiguousarray(distance, np.float32)
+        out = np.zeros(len(s), np.uint8)
+        blocks = np.zeros(len(s), np.int32)
+        self.port.lib.vgo_validate_vectors(robot.h, self.h, lanes, _ptr(s), _ptr(v), _ptr(d), len(s), resolution,
+                                           _ptr(out), _ptr(blocks), threads)
+        return out, blocks
+
     def validate_motions_counted(self, robot: PortRobot, a, b, resolution: int, lanes: int = 8):
         a = np.ascontiguousarray(a, np.float32)
         b = np.ascontiguousarray(b, np.float32)
@@ -368,6 +381,7 @@ class Reference:
             getattr(lib, f"vgref_{r}_fkcc_block").argtypes = [_p, _p]
             getattr(lib, f"vgref_{r}_validate_states").argtypes = [_p, _p, _sz, _p, ctypes.c_int]
             getattr(lib, f"vgref_{r}_validate_motions").argtypes = [_p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
+            getattr(lib, f"vgref_{r}_validate_vectors").argtypes = [_p, _p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
             getattr(lib, f"vgref_{r}_motion_blocks").argtypes = [_p, _p, ctypes.c_int, _p, _sz, ctypes.c_long]
             getattr(lib, f"vgref_{r}_motion_blocks").restype = ctypes.c_long
             getattr(lib, f"vgref_{r}_sphere_fk").argtypes = [_p, _p]
@@ -479,6 +493,15 @@ class RefEnv:
             fn(self.h, _ptr(q[i]), _ptr(bits[i]), words, _ptr(buf), cap, ctypes.byref(cnt))
             out_pairs.append([(int(buf[2 * k]), int(buf[2 * k + 1])) for k in range(min(cnt.value, cap))])
         return bits, out_pairs
+
+    def validate_vectors(self, robot: str, start, vector, distance, resolution: int, threads: int = 1):
+        s = np.ascontiguousarray(start, np.float32)
+        v = np.ascontiguousarray(vector, np.float32)
+        d = np.ascontiguousarray(distance, np.float32)
+        out = np.zeros(len(s), np.uint8)
+        getattr(self.ref.lib, f"vgref_{robot}_validate_vectors")(self.h, _ptr(s), _ptr(v), _ptr(d), len(s), resolution,
+                                                                _ptr(out), threads)
+        return out
 
     def validate_states(self, robot: str, q, threads: int = 1):
         q = np.ascontiguousarray(q, np.float32)

@@ -109,10 +109,29 @@ def heightfield_fixtures(ref: Reference) -> None:
                         state_verdict=renv.validate_states("panda", q))
 
 
+def vector_fixtures(ref: Reference) -> None:
+    """validate_vector (planning/validate.hh:23-63) as the planners call it: a start, a vector (an
+    extension of at most 1.5 rad here) and the distance that sets the block count, half the time
+    the vector's own length (float32 norm) and half the time another value."""
+    for r, scene, seed in (("panda", scenes.scene_config1(5), 95), ("ur5", scenes.scene_config1(6), 96)):
+        rb = Port().robot(r)
+        rng = np.random.default_rng(seed)
+        a, b = scenes.edges(rb.s_m, rb.s_a, 1024, seed)
+        v = (b - a).astype(np.float32)
+        norm = np.linalg.norm(v.astype(np.float64), axis=1)
+        scale = np.minimum(1.0, 1.5 / np.maximum(norm, 1e-9))
+        v = (v * scale[:, None]).astype(np.float32)
+        d = np.linalg.norm(v.astype(np.float64), axis=1).astype(np.float32)
+        other = rng.random(len(d)) < 0.5
+        d[other] = (d[other] * rng.uniform(0.3, 2.0, other.sum())).astype(np.float32)
+        verdict = ref.env(scene).validate_vectors(r, a, v, d, 32)
+        np.savez_compressed(OUT / f"vectors_{r}.npz", start=a, vector=v, distance=d, verdict=verdict, **scene_arrays(scene))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None)
-    ap.add_argument("--only", choices=["filter", "eefk", "heightfield"], default=None,
+    ap.add_argument("--only", choices=["filter", "eefk", "heightfield", "vectors"], default=None,
                     help="regenerate one group of fixtures")
     a = ap.parse_args()
     if build_reference(a.reference) is None:
@@ -125,6 +144,8 @@ def main():
         eefk_fixtures(Path(a.reference or "/root/reference"))
     if a.only in (None, "heightfield"):
         heightfield_fixtures(ref)
+    if a.only in (None, "vectors"):
+        vector_fixtures(ref)
     if a.only is not None:
         return
 

@@ -241,3 +241,13 @@ def test_heightfield_matches_the_reference(port):
     assert np.array_equal(env.sphere_env(g["mixed"]), g["mixed_verdict"])
     assert np.array_equal(env.validate_states(port.robot("panda"), g["q"]), g["state_verdict"])
     assert 0.1 < g["single_verdict"].mean() < 0.9 and 0.1 < g["state_verdict"].mean() < 0.95
+
+
+@pytest.mark.parametrize("robot", ["panda", "ur5"])
+def test_validate_vector_matches_the_reference(port, robot):
+    """validate_vector with caller-given distances (golden fixture from the compiled reference)."""
+    g = golden(f"vectors_{robot}")
+    env = port.env(scene_of(g))
+    out, _ = env.validate_vectors(port.robot(robot), g["start"], g["vector"], g["distance"], 32)
+    assert np.array_equal(out, g["verdict"])
+    assert 0.1 < g["verdict"].mean() < 0.95

@@ -284,6 +284,30 @@ class Robot:
         check(lib.vg_validate_motions(self._b, environment.handle, _ptr(a), _ptr(b), len(a), res, _ptr(out)))
         return out
 
+    def validate_vector_batch(self, starts, vectors, distances, environment: Environment, resolution: int | None = None,
+                              out=None, blocks=None):
+        """validate_vector (planning/validate.hh:23-63) for every edge: from starts[i] along
+        vectors[i], checked in max(ceil(distances[i] / lanes * resolution), 1) blocks, distances[i]
+        being the length the caller gives (the reference's planners pass their extension
+        length)."""
+        res = self._res if resolution is None else int(resolution)
+        if _is_cuda_tensor(starts):
+            import torch
+
+            a, v, d = starts.contiguous(), vectors.contiguous(), distances.to(torch.float32).contiguous()
+            n = a.shape[0]
+            out = torch.empty(n, dtype=torch.uint8, device=a.device) if out is None else out
+            bp = blocks.data_ptr() if blocks is not None else None
+            check(lib.vg_validate_vectors_device(self._b, environment.handle, a.data_ptr(), v.data_ptr(), d.data_ptr(), n,
+                                                 res, out.data_ptr(), bp, torch.cuda.current_stream(a.device).cuda_stream))
+            return out
+        a = np.ascontiguousarray(starts, np.float32).reshape(-1, self._dim)
+        v = np.ascontiguousarray(vectors, np.float32).reshape(-1, self._dim)
+        d = np.ascontiguousarray(distances, np.float32).reshape(-1)
+        out = np.zeros(len(a), np.uint8) if out is None else out
+        check(lib.vg_validate_vectors(self._b, environment.handle, _ptr(a), _ptr(v), _ptr(d), len(a), res, _ptr(out)))
+        return out
+
     def debug(self, configuration, environment: Environment):
         """Which objects each fine sphere collides with and which fine self pairs collide, for one
         configuration (the reference binding's debug(), bindings/robot_helper.hh:249-253): a list

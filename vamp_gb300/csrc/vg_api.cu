@@ -416,7 +416,8 @@ namespace vg
         const int per_block = grouped ? kBlock / 32 : kBlock / env->lanes;
         const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
         const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
-        EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes};
+        EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes,
+                      m.dist};
         const auto launch = ext ? r->edges_ext[which]
                                    : learned ? r->edges_learned[which]
                                              : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
@@ -850,6 +851,37 @@ int vg_validate_motions_device(
     return launch_motions(m, static_cast<cudaStream_t>(stream));
 }
 
+// planning::validate_vector<Robot, lanes, resolution> (planning/validate.hh:23-63) for a batch:
+// edge e starts at start[e], moves by vector[e], and is checked in max(ceil(distance[e] / lanes
+// * resolution), 1) blocks, whatever the vector's length (the reference's planners pass the
+// extension length they chose).  Same schedules and outputs as vg_validate_motions_device.
+int vg_validate_vectors_device(
+    const char *robot,
+    vg_env *env,
+    const float *start,
+    const float *vector,
+    const float *distance,
+    size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!start || !vector || !distance || !out)) || resolution < 1)
+        return set_error(VG_ERR_ARG, "vg_validate_vectors_device: bad argument");
+    if (n > 0x7fffffffu)
+        return set_error(VG_ERR_LIMIT, "vg_validate_vectors_device: more than 2^31 - 1 edges");
+    if (n == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    MotionLaunch m{r, env, start, vector, n, resolution, nullptr, 0, out, blocks, env->d_counter};
+    m.dist = distance;
+    tuned_for(env, r, &m.schedule, &m.blocks_per_sm);
+    return launch_motions(m, static_cast<cudaStream_t>(stream));
+}
+
 // Same verdicts as vg_validate_motions_device, with each edge's blocks checked in the order its
 // collision scores rank them (scores[e * probes + p]: any monotone collision score of the state at
 // fraction (p + 0.5) / probes along edge e, e.g. an MLP's logit).  The order is a permutation of
@@ -973,6 +1005,33 @@ int vg_validate_motions(
     VG_CUDA(cudaMemcpyAsync(da, a, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy starts");
     VG_CUDA(cudaMemcpyAsync(db, b, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy goals");
     if (int rc = vg_validate_motions_device(robot, env, da, db, n, resolution, dout, nullptr, nullptr))
+        return rc;
+    VG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, 0), "copy verdicts");
+    VG_CUDA(cudaStreamSynchronize(0), "synchronize");
+    return VG_OK;
+}
+
+int vg_validate_vectors(const char *robot, vg_env *env, const float *start, const float *vector, const float *distance,
+                        size_t n, int resolution, uint8_t *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n && (!start || !vector || !distance || !out)))
+        return set_error(VG_ERR_ARG, "vg_validate_vectors: bad argument");
+    if (n == 0)
+        return VG_OK;
+    const size_t cb = ((n * r->dim * sizeof(float)) + 255) & ~size_t(255);
+    const size_t db_ = ((n * sizeof(float)) + 255) & ~size_t(255);
+    if (int rc = ensure_stage(env, 2 * cb + db_ + n))
+        return rc;
+    char *base = static_cast<char *>(env->d_stage);
+    float *ds = reinterpret_cast<float *>(base);
+    float *dv = reinterpret_cast<float *>(base + cb);
+    float *dd = reinterpret_cast<float *>(base + 2 * cb);
+    uint8_t *dout = reinterpret_cast<uint8_t *>(base + 2 * cb + db_);
+    VG_CUDA(cudaMemcpyAsync(ds, start, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy starts");
+    VG_CUDA(cudaMemcpyAsync(dv, vector, n * r->dim * sizeof(float), cudaMemcpyHostToDevice, 0), "copy vectors");
+    VG_CUDA(cudaMemcpyAsync(dd, distance, n * sizeof(float), cudaMemcpyHostToDevice, 0), "copy distances");
+    if (int rc = vg_validate_vectors_device(robot, env, ds, dv, dd, n, resolution, dout, nullptr, nullptr))
         return rc;
     VG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, 0), "copy verdicts");
     VG_CUDA(cudaStreamSynchronize(0), "synchronize");

@@ -147,6 +147,7 @@ namespace vg
         unsigned *counter;     // work counter, cleared on the stream before the launch
         int schedule = 1;      // 0: a segment per edge, 1: a warp per edge, 2: the same, register-rich build
         int blocks_per_sm = 0;  // 0: as many as fit
+        const float *dist = nullptr;  // validate_vector form: b holds vectors, dist their lengths
     };
 
     int commit(vg_env *e);

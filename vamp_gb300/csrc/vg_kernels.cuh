@@ -220,7 +220,7 @@ namespace vg
     struct EdgesParams
     {
         const float *a;  // [n][dim] start configurations
-        const float *b;  // [n][dim] goal configurations
+        const float *b;  // [n][dim] goal configurations (with dist: the motion vectors)
         int n;
         int resolution;
         uint8_t *out;        // 1 = valid
@@ -231,6 +231,9 @@ namespace vg
         // at fractions (p + 0.5) / probes along the edge; null = the reference's block order
         const float *scores;
         int probes;
+        // validate_vector form (planning/validate.hh:23-63): b holds each edge's vector and dist
+        // its length as the caller gives it (the block count follows it); null = validate_motion
+        const float *dist = nullptr;
     };
 
     constexpr int kOrderMax = 64;  // blocks of an edge the learned order ranks; later ones follow in order
@@ -371,9 +374,10 @@ namespace vg
                     for (int d = 0; d < D; ++d)
                     {
                         av[d] = p.a[static_cast<long long>(e) * D + d];
-                        v[d] = __fsub_rn(p.b[static_cast<long long>(e) * D + d], av[d]);
+                        v[d] = p.dist ? p.b[static_cast<long long>(e) * D + d]
+                                      : __fsub_rn(p.b[static_cast<long long>(e) * D + d], av[d]);
                     }
-                    const float len = edge_length<D>(v);
+                    const float len = p.dist ? p.dist[e] : edge_length<D>(v);
                     const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
                     const float nf = ceilf(t);
                     n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
@@ -474,10 +478,11 @@ namespace vg
             for (int d = 0; d < D; ++d)
             {
                 const float av = p.a[static_cast<long long>(e) * D + d];
-                v[d] = __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
+                v[d] = p.dist ? p.b[static_cast<long long>(e) * D + d]
+                              : __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
                 q[d] = __fmaf_rn(v[d], pct, av);
             }
-            const float len = edge_length<D>(v);
+            const float len = p.dist ? p.dist[e] : edge_length<D>(v);
             const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
             const float nf = ceilf(t);
             const int n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
@@ -630,10 +635,11 @@ namespace vg
                     for (int d = 0; d < D; ++d)
                     {
                         const float av = p.a[static_cast<long long>(e) * D + d];
-                        v[d] = __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
+                        v[d] = p.dist ? p.b[static_cast<long long>(e) * D + d]
+                                      : __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
                         q[d] = __fmaf_rn(v[d], pct, av);
                     }
-                    const float len = edge_length<D>(v);
+                    const float len = p.dist ? p.dist[e] : edge_length<D>(v);
                     const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
                     const float nf = ceilf(t);
                     n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
