@@ -10,8 +10,10 @@
 //      forward scan that skips 32-, 1024- and 32768-entry tiles whose bounding box lies inside
 //      the min_dist ball (tested in double with a margin, so a skipped entry is never "far");
 //   4. the kept entries are the chain 0, next[0], next[next[0]], ...: per 1024-entry chunk,
-//      pointer doubling gives the first chain element past the chunk from every entry; one
-//      thread walks the chunks; each chunk then marks its own chain members;
+//      pointer doubling gives the first chain element past the chunk from every entry; those
+//      exits, composed over 16 chunks, let one thread walk the chain a superchunk at a time and
+//      a thread per superchunk find its chunks' entry points; each chunk then marks its own
+//      chain members (binary lifting over its doubling tables);
 //   5. an ordered compaction of the kept entries gives the next pass's list.
 // The reference's list has n entries, and those past the points that pass the cull hold index 0
 // (filter.hh:199-216).  Those copies are identical (same point, same code, adjacent after the
@@ -477,21 +479,61 @@ namespace vg
                 exit_of[c0 + t] = src[t];
         }
 
-        // the chain's entry point into each chunk it visits (one thread; chunks it skips keep
-        // 0xFFFFFFFF)
-        __global__ void chain_walk(const uint32_t *exit_of, long long m, uint32_t *entry, uint32_t *err)
+        constexpr int kSuper = 16;  // chunks per superchunk of the chain walk
+
+        // exit_super[e]: the first chain element past the superchunk of e (kSuper chunks), from e:
+        // at most kSuper hops, each leaving a chunk
+        __global__ void super_exit(const uint32_t *exit_of, long long m, uint32_t *exit_super, uint32_t *err)
         {
-            long long e = 0;
-            while (e < m)
+            const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (e >= m)
+                return;
+            const long long end = (e / (kTile * kSuper) + 1) * (kTile * kSuper);
+            long long x = e;
+            for (int h = 0; h < kSuper + 1 && x < end && x < m; ++h)
             {
-                entry[e / kTile] = static_cast<uint32_t>(e);
-                const long long x = exit_of[e];  // past e's chunk
-                if (x < (e / kTile + 1) * kTile && x < m)
+                const long long y = exit_of[x];
+                if (y < (x / kTile + 1) * kTile && y < m)
                 {
                     *err = 1u;  // not reached: every exit leaves its chunk
                     return;
                 }
+                x = y;
+            }
+            exit_super[e] = static_cast<uint32_t>(x < m ? x : m);
+        }
+
+        // the chain's entry point into each superchunk it visits (one thread, one step per
+        // superchunk; superchunks it skips keep 0xFFFFFFFF)
+        __global__ void chain_walk(const uint32_t *exit_super, long long m, uint32_t *entry_super, uint32_t *err)
+        {
+            long long e = 0;
+            while (e < m)
+            {
+                entry_super[e / (kTile * kSuper)] = static_cast<uint32_t>(e);
+                const long long x = exit_super[e];
+                if (x < (e / (kTile * kSuper) + 1) * (kTile * kSuper) && x < m)
+                {
+                    *err = 1u;  // not reached: every exit leaves its superchunk
+                    return;
+                }
                 e = x;
+            }
+        }
+
+        // the chain's entry point into each chunk of one superchunk (a thread per superchunk)
+        __global__ void chunk_entries(const uint32_t *exit_of, long long m, const uint32_t *entry_super,
+                                      long long supers, uint32_t *entry)
+        {
+            const long long sc = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (sc >= supers || entry_super[sc] == 0xFFFFFFFFu)
+                return;
+            const long long end = (sc + 1) * (kTile * kSuper);
+            long long x = entry_super[sc];
+            for (int h = 0; h < kSuper && x < end && x < m; ++h)
+            {
+                entry[x / kTile] = static_cast<uint32_t>(x);
+                x = exit_of[x];  // leaves x's chunk (checked by super_exit)
             }
         }
 
@@ -596,6 +638,7 @@ namespace vg
             uint32_t *sums = fb.get<uint32_t>(tiles), *offs = fb.get<uint32_t>(tiles + 1);
             uint32_t *sidx = fb.get<uint32_t>(N + 1), *next = fb.get<uint32_t>(N + 1), *exit_of = fb.get<uint32_t>(N + 1);
             uint32_t *entry = fb.get<uint32_t>(tiles);
+            uint32_t *exit_super = fb.get<uint32_t>(N + 1), *entry_super = fb.get<uint32_t>(blocks_of(tiles, kSuper));
             unsigned long long *keys = fb.get<unsigned long long>(M);
             float4 *sp = fb.get<float4>(N + 1);
             Box *b32 = fb.get<Box>(blocks_of(N + 1, 32)), *b1k = fb.get<Box>(blocks_of(N + 1, 1024)),
@@ -671,8 +714,12 @@ namespace vg
                 next_kernel<<<blocks_of(m, 128), 128, 0, s>>>(NextParams{sp, m, sq, limit, b32, b1k, b32k, next});
                 const long long chunks = blocks_of(m, kTile);
                 chunk_exit<<<static_cast<unsigned>(chunks), kTile, 0, s>>>(next, m, exit_of);
+                const long long supers = blocks_of(chunks, kSuper);
                 VG_CUDA(cudaMemsetAsync(entry, 0xFF, chunks * sizeof(uint32_t), s), "vg_filter_pointcloud: memset");
-                chain_walk<<<1, 1, 0, s>>>(exit_of, m, entry, err);
+                VG_CUDA(cudaMemsetAsync(entry_super, 0xFF, supers * sizeof(uint32_t), s), "vg_filter_pointcloud: memset");
+                super_exit<<<blocks_of(m, 256), 256, 0, s>>>(exit_of, m, exit_super, err);
+                chain_walk<<<1, 1, 0, s>>>(exit_super, m, entry_super, err);
+                chunk_entries<<<blocks_of(supers, 128), 128, 0, s>>>(exit_of, m, entry_super, supers, entry);
                 mark_kept<<<static_cast<unsigned>(chunks), kTile, 0, s>>>(next, m, entry, flags, err);
                 tile_sums<<<static_cast<unsigned>(chunks), kTile, 0, s>>>(flags, m, sums);
                 scan_tiles<<<1, kTile, 0, s>>>(sums, chunks, offs);
