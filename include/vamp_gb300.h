@@ -77,7 +77,8 @@ int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, 
 /* The same tree as vg_env_add_pointcloud, built on the current GPU (no counterpart in the
  * reference, whose CAPT is built on the host: collision/capt.hh:294-365): xyz is a device array
  * [n][3] on that GPU; the call returns once the tree is built (synchronous on `stream`, a
- * cudaStream_t or NULL).  The layout is bit-identical to the host build's. */
+ * cudaStream_t or NULL).  The layout is bit-identical to the host build's.  Points must be
+ * finite (as for the host build, whose median sort is undefined for NaN). */
 int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point,
                                  void *stream);
 /* The reference's pointcloud filter on the current GPU (collision/filter.hh:176-320,
@@ -90,7 +91,9 @@ int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float 
  * kept points go to out (capacity n points), their number to *n_out.
  *   _device: xyz and out on the current GPU; synchronous on `stream` (a cudaStream_t or NULL).
  *   host form: xyz and out in host memory; *elapsed_ns (if non-NULL) gets the call's wall time,
- *   as the reference's binding returns it. */
+ *   as the reference's binding returns it.
+ * Coordinates must be finite.  Runs of more than 32,768 consecutive points within min_dist of one
+ * another cost time in proportion to their length (the tile skipping handles the rest). */
 int vg_filter_pointcloud_device(const float *xyz, size_t n, float min_dist, float max_range, const float *origin,
                                 const float *workcell_min, const float *workcell_max, int cull, float *out, size_t *n_out,
                                 void *stream);
