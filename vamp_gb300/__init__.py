@@ -4,7 +4,8 @@ The Python surface mirrors the reference's bindings (src/impl/vamp/bindings/robo
 environment.cc): an `Environment` built from primitives, and one object per robot (`panda`,
 `ur5`, `fetch`, `baxter`) with `validate`, `validate_motion`, `fk`, `min_max_radii`,
 `dimension`, `resolution`, plus batched `validate_batch` / `validate_motion_batch`;
-`filter_pointcloud` (environment.cc:167-197) on the GPU; and, with
+`filter_pointcloud` (environment.cc:167-197) on the GPU, `Attachment`, `HeightField`, each
+robot's `eefk` and `validate_vector_batch` (planning/validate.hh:23-63); and, with
 no counterpart in the reference, `autotune`, `Batch` (checks replayed as one CUDA graph) and
 `CollisionPredictor` (the learned block ordering).
 
