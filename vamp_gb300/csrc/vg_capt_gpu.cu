@@ -72,6 +72,56 @@ namespace vg
             }
         }
 
+        constexpr int kSortTile = 2048;  // entries per shared-memory tile of the sort
+
+        // All compare-exchange stages of sizes k in [k0, k1] and strides below the tile, on tiles
+        // of T = min(S, 2048) entries (S: the sorted segment size, a power of two).
+        __global__ void bitonic_tile(float *key, uint32_t *pos, uint32_t *ord, long long S, long long k0, long long k1)
+        {
+            __shared__ float sk[kSortTile];
+            __shared__ uint32_t sp[kSortTile], so[kSortTile];
+            const long long T = S < kSortTile ? S : kSortTile;
+            const long long base = static_cast<long long>(blockIdx.x) * T;
+            for (long long t = threadIdx.x; t < T; t += blockDim.x)
+            {
+                sk[t] = key[base + t];
+                sp[t] = pos[base + t];
+                so[t] = ord[base + t];
+            }
+            __syncthreads();
+            for (long long k = k0; k <= k1; k <<= 1)
+            {
+                for (long long j = (k >> 1) < (T >> 1) ? (k >> 1) : (T >> 1); j > 0; j >>= 1)
+                {
+                    for (long long t = threadIdx.x; t < (T >> 1); t += blockDim.x)
+                    {
+                        const long long i = 2 * t - (t & (j - 1)), q = i + j;
+                        const bool up = k == S || ((base + i) & k) == 0;
+                        const float ki = sk[i], kq = sk[q];
+                        const bool greater = ki > kq || (ki == kq && sp[i] > sp[q]);
+                        if (greater == up)
+                        {
+                            sk[i] = kq;
+                            sk[q] = ki;
+                            const uint32_t a = sp[i];
+                            sp[i] = sp[q];
+                            sp[q] = a;
+                            const uint32_t o = so[i];
+                            so[i] = so[q];
+                            so[q] = o;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (long long t = threadIdx.x; t < T; t += blockDim.x)
+            {
+                key[base + t] = sk[t];
+                pos[base + t] = sp[t];
+                ord[base + t] = so[t];
+            }
+        }
+
         struct NodeInfo
         {
             float up, down;
@@ -523,9 +573,16 @@ namespace vg
         {
             const long long nodes = 1ll << d, S = N >> d;
             load_keys<<<grid_of(N, 256), 256, 0, s>>>(ord, axis[d % 3], N, key, pos);
-            for (long long k = 2; k <= S; k <<= 1)
-                for (long long j = k >> 1; j > 0; j >>= 1)
+            // strides below the tile in shared memory, the longer ones one launch each
+            const long long T = std::min<long long>(S, kSortTile);
+            const unsigned tiles = static_cast<unsigned>(N / T), threads = static_cast<unsigned>(std::max<long long>(T / 2, 1));
+            bitonic_tile<<<tiles, threads, 0, s>>>(key, pos, ord, S, 2, T);
+            for (long long k = 2 * T; k <= S; k <<= 1)
+            {
+                for (long long j = k >> 1; j >= T; j >>= 1)
                     bitonic_stage<<<grid_of(N, 256), 256, 0, s>>>(key, pos, ord, N, k, j, S);
+                bitonic_tile<<<tiles, threads, 0, s>>>(key, pos, ord, S, k, k);
+            }
             split_nodes<<<grid_of(nodes, 128), 128, 0, s>>>(key, N, d, r_max, cell, out.tests, info, child_cell);
             count_children<<<static_cast<unsigned>(nodes), kListBlock, 0, s>>>(off, items, axis[d % 3], N, d, info, sizes);
             scan_small<<<1, 1024, 0, s>>>(sizes, 2 * nodes, child_off);
