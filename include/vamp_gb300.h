@@ -100,6 +100,15 @@ int vg_filter_pointcloud_device(const float *xyz, size_t n, float min_dist, floa
 int vg_filter_pointcloud(const float *xyz, size_t n, float min_dist, float max_range, const float *origin,
                          const float *workcell_min, const float *workcell_max, int cull, float *out, size_t *n_out,
                          uint64_t *elapsed_ns);
+/* filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): the points of xyz[n][3], as
+ * spheres of point_radius, that collide with no fine sphere of the robot at configuration
+ * q[dim] (a host array) and with no object of env, in input order, to out (capacity n); their
+ * number to *n_out.  _device: xyz and out on the GPU, synchronous on `stream`; host form: host
+ * buffers. */
+int vg_filter_self_from_pointcloud_device(const char *robot, vg_env *env, const float *xyz, size_t n, float point_radius,
+                                          const float *q, float *out, size_t *n_out, void *stream);
+int vg_filter_self_from_pointcloud(const char *robot, vg_env *env, const float *xyz, size_t n, float point_radius,
+                                   const float *q, float *out, size_t *n_out);
 /* The tree of the index-th pointcloud (collision/capt.hh:584-617): sizes = {nlog2, tests,
  * leaves, 8-point blocks}; then, if non-NULL, tests[tests], aabbs[leaves][6], aff_starts[leaves
  * + 1], aff[blocks][3][8] (x, y, z planes of each block), top[6].  Call with NULL arrays for the

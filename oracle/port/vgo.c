@@ -649,6 +649,39 @@ int vgo_fkcc(const vgo_robot *r, const vgo_env *e, int lanes, const float *q)
     return 1;
 }
 
+/* filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): the points (spheres of
+ * radius point_radius) that collide with no fine sphere of the robot at configuration q
+ * (sphere_sphere_sql2 < 0) and with no environment object (sphere_environment_in_collision, one
+ * lane), in input order.  The scalar test's rounding is taken as fma(dz, dz, fma(dx, dx, dy*dy))
+ * - rs*rs. */
+size_t vgo_filter_self(const vgo_robot *r, const vgo_env *e, const float *xyz, size_t n, float point_radius,
+                       const float *q, float *out)
+{
+    float S[VGO_MAX_SLOTS * 4];
+    r->f32(q, S);
+    size_t m = 0;
+    for (size_t i = 0; i < n; ++i)
+    {
+        const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2], rad = point_radius;
+        int valid = 1;
+        for (int k = 0; k < r->fine && valid; ++k)
+        {
+            const float *s = S + 4 * k;
+            const float dx = s[0] - x, dy = s[1] - y, dz = s[2] - z, rs = s[3] + rad;
+            if (fmaf(dz, dz, fmaf(dx, dx, dy * dy)) - rs * rs < 0.0f)
+                valid = 0;
+        }
+        if (valid && vgo_sphere_env(e, 1, &x, &y, &z, &rad))
+            valid = 0;
+        if (valid)
+        {
+            memcpy(out + 3 * m, xyz + 3 * i, 3 * sizeof(float));
+            ++m;
+        }
+    }
+    return m;
+}
+
 /* ======================================================================= motion validation */
 
 /* |b - a| as the reference computes it on x86: squares summed lane-wise across the 8-wide

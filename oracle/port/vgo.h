@@ -70,6 +70,10 @@ int vgo_robot_self_pairs(const vgo_robot *r);
 /* Robot::fkcc_debug for one configuration: env_words [fine][words] (bit = insertion id of an
  * object the sphere collides with), pairs [self pairs] (1 = the fine pair collides) */
 void vgo_debug(const vgo_robot *r, const vgo_env *e, const float *q, uint32_t *env_words, int words, uint8_t *pairs);
+/* filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): kept points to out (capacity
+ * n), returns their number */
+size_t vgo_filter_self(const vgo_robot *r, const vgo_env *e, const float *xyz, size_t n, float point_radius,
+                       const float *q, float *out);
 /* ------------------------------------------------------------------------------------- queries */
 /* sphere_environment_in_collision over one block of `lanes` spheres (validity.hh:47-150) */
 int vgo_sphere_env(const vgo_env *e, int lanes, const float *x, const float *y, const float *z, const float *r);

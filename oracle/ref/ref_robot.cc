@@ -311,6 +311,44 @@ void VG_FN(_validate_vectors)(
         });
 }
 
+// filter_self_from_pointcloud as the binding computes it (bindings/robot_helper.hh:307-345), from
+// the reference's own sphere_fk<1>, sphere_sphere_sql2 and sphere_environment_in_collision.
+// Writes the kept points to out (capacity n); returns their number.
+std::size_t VG_FN(_filter_self)(void *env, const float *xyz, std::size_t n, float point_radius, const float *q, float *out)
+{
+    auto *e = static_cast<RefEnv *>(env);
+    e->finalize();
+    const auto &ev = *e->vec;
+    typename Robot::template Spheres<1> s;
+    typename Robot::template ConfigurationBlock<1> block;
+    for (std::size_t d = 0; d < Robot::dimension; ++d)
+        block[d] = FloatVector<1, 1>::fill(q[d]);
+    Robot::template sphere_fk<1>(block, s);
+    std::size_t m = 0;
+    for (std::size_t i = 0; i < n; ++i)
+    {
+        const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2], r = point_radius;
+        bool valid = true;
+        for (auto k = 0U; k < Robot::n_spheres; ++k)
+        {
+            if (collision::sphere_sphere_sql2(s.x[{k, 0}], s.y[{k, 0}], s.z[{k, 0}], s.r[{k, 0}], x, y, z, r) < 0 or
+                sphere_environment_in_collision<>(ev, x, y, z, r))
+            {
+                valid = false;
+                break;
+            }
+        }
+        if (valid)
+        {
+            out[3 * m] = x;
+            out[3 * m + 1] = y;
+            out[3 * m + 2] = z;
+            ++m;
+        }
+    }
+    return m;
+}
+
 // The blocks validate_motion visits for one edge, in visiting order.  out holds up to cap blocks of
 // [dim][lanes] floats.  If fail_at >= 0 the fail_at-th visited block reports a collision, which
 // shows where the reference stops.  Returns the number of blocks visited.

@@ -141,6 +141,8 @@ class Port:
         lib.vgo_robot_self_pairs.argtypes = [_p]
         lib.vgo_debug.argtypes = [_p, _p, _p, _p, ctypes.c_int, _p]
         lib.vgo_env_add_heightfield.argtypes = [_p, _p, _p, ctypes.c_int, ctypes.c_int, _p]
+        lib.vgo_filter_self.argtypes = [_p, _p, _p, _sz, _f, _p, _p]
+        lib.vgo_filter_self.restype = _sz
         lib.vgo_validate_vectors.argtypes = [_p, _p, ctypes.c_int, _p, _p, _p, _sz, ctypes.c_int, _p, _p, ctypes.c_int]
         lib.vgo_env_attach.argtypes = [_p, _p, _p, ctypes.c_int]
         lib.vgo_env_detach.argtypes = [_p]
@@ -303,6 +305,14 @@ class PortEnv:
         q = np.ascontiguousarray(q, np.float32)
         return self.port.lib.vgo_fkcc(robot.h, self.h, q.shape[0], _ptr(q))
 
+    def filter_self(self, robot: PortRobot, points, point_radius: float, q) -> np.ndarray:
+        """filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): the kept points."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        qq = np.ascontiguousarray(q, np.float32)
+        m = self.port.lib.vgo_filter_self(robot.h, self.h, _ptr(pts), len(pts), point_radius, _ptr(qq), _ptr(out))
+        return out[:m].copy()
+
     def validate_vectors(self, robot: PortRobot, start, vector, distance, resolution: int, lanes: int = 8,
                          threads: int = 1):
         """validate_vector (planning/validate.hh:23-63) per edge: (verdicts, blocks checked)."""
@@ -381,6 +391,8 @@ class Reference:
             getattr(lib, f"vgref_{r}_fkcc_block").argtypes = [_p, _p]
             getattr(lib, f"vgref_{r}_validate_states").argtypes = [_p, _p, _sz, _p, ctypes.c_int]
             getattr(lib, f"vgref_{r}_validate_motions").argtypes = [_p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
+            getattr(lib, f"vgref_{r}_filter_self").argtypes = [_p, _p, _sz, _f, _p, _p]
+            getattr(lib, f"vgref_{r}_filter_self").restype = _sz
             getattr(lib, f"vgref_{r}_validate_vectors").argtypes = [_p, _p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
             getattr(lib, f"vgref_{r}_motion_blocks").argtypes = [_p, _p, ctypes.c_int, _p, _sz, ctypes.c_long]
             getattr(lib, f"vgref_{r}_motion_blocks").restype = ctypes.c_long
@@ -493,6 +505,14 @@ class RefEnv:
             fn(self.h, _ptr(q[i]), _ptr(bits[i]), words, _ptr(buf), cap, ctypes.byref(cnt))
             out_pairs.append([(int(buf[2 * k]), int(buf[2 * k + 1])) for k in range(min(cnt.value, cap))])
         return bits, out_pairs
+
+    def filter_self(self, robot: str, points, point_radius: float, q) -> np.ndarray:
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        qq = np.ascontiguousarray(q, np.float32)
+        m = getattr(self.ref.lib, f"vgref_{robot}_filter_self")(self.h, _ptr(pts), len(pts), point_radius, _ptr(qq),
+                                                                _ptr(out))
+        return out[:m].copy()
 
     def validate_vectors(self, robot: str, start, vector, distance, resolution: int, threads: int = 1):
         s = np.ascontiguousarray(start, np.float32)

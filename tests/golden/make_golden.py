@@ -128,10 +128,32 @@ def vector_fixtures(ref: Reference) -> None:
         np.savez_compressed(OUT / f"vectors_{r}.npz", start=a, vector=v, distance=d, verdict=verdict, **scene_arrays(scene))
 
 
+def filter_self_fixtures(ref: Reference) -> None:
+    """filter_self_from_pointcloud (bindings/robot_helper.hh:307-345) of a cloud around the Panda
+    at a few configurations, in the 60-primitive scene."""
+    rng = np.random.default_rng(97)
+    scene = scenes.scene_config1(8)
+    rb = Port().robot("panda")
+    q = scenes.configurations(rb.s_m, rb.s_a, 4, 98)
+    pts = rng.uniform([-0.8, -0.8, 0.0], [0.8, 0.8, 1.2], (6000, 3)).astype(np.float32)
+    # and points around the robot's fine spheres at the first configuration, half inside reach
+    sph = rb.spheres_f64(q[0].astype(np.float64))[: rb.fine]
+    k = rng.integers(0, rb.fine, 3000)
+    u = rng.normal(size=(3000, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    near = sph[k, :3] + u * (sph[k, 3] + 0.01 + rng.uniform(-0.01, 0.01, 3000))[:, None]
+    pts = np.concatenate([pts, near.astype(np.float32)])
+    renv = ref.env(scene)
+    out = {"q": q, "points": pts, "radius": np.float32(0.01), **scene_arrays(scene)}
+    for i, qi in enumerate(q):
+        out[f"kept{i}"] = renv.filter_self("panda", pts, 0.01, qi)
+    np.savez_compressed(OUT / "filter_self_panda.npz", **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None)
-    ap.add_argument("--only", choices=["filter", "eefk", "heightfield", "vectors"], default=None,
+    ap.add_argument("--only", choices=["filter", "eefk", "heightfield", "vectors", "filter_self"], default=None,
                     help="regenerate one group of fixtures")
     a = ap.parse_args()
     if build_reference(a.reference) is None:
@@ -146,6 +168,8 @@ def main():
         heightfield_fixtures(ref)
     if a.only in (None, "vectors"):
         vector_fixtures(ref)
+    if a.only in (None, "filter_self"):
+        filter_self_fixtures(ref)
     if a.only is not None:
         return
 

@@ -251,3 +251,14 @@ def test_validate_vector_matches_the_reference(port, robot):
     out, _ = env.validate_vectors(port.robot(robot), g["start"], g["vector"], g["distance"], 32)
     assert np.array_equal(out, g["verdict"])
     assert 0.1 < g["verdict"].mean() < 0.95
+
+
+def test_filter_self_matches_the_reference(port):
+    """filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): uniform points and points
+    around the robot's spheres (golden fixture from the compiled reference)."""
+    g = golden("filter_self_panda")
+    env = port.env(scene_of(g))
+    for i in range(len(g["q"])):
+        kept = env.filter_self(port.robot("panda"), g["points"], float(g["radius"]), g["q"][i])
+        assert kept.shape == g[f"kept{i}"].shape and np.array_equal(kept, g[f"kept{i}"]), i
+    assert len(g["kept0"]) < 0.8 * len(g["points"])  # the robot removes many of the near points

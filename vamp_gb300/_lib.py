@@ -47,6 +47,8 @@ def _load() -> ctypes.CDLL:
         "vg_env_add_heightfield": ([_p, _p, _p, _sz, _sz, _p], _i),
         "vg_validate_vectors_device": ([ctypes.c_char_p, _p, _p, _p, _p, _sz, _i, _p, _p, _p], _i),
         "vg_validate_vectors": ([ctypes.c_char_p, _p, _p, _p, _p, _sz, _i, _p], _i),
+        "vg_filter_self_from_pointcloud_device": ([ctypes.c_char_p, _p, _p, _sz, _f, _p, _p, _p, _p], _i),
+        "vg_filter_self_from_pointcloud": ([ctypes.c_char_p, _p, _p, _sz, _f, _p, _p, _p], _i),
         "vg_env_attach": ([_p, _p, _p, _sz], _i),
         "vg_env_detach": ([_p], _i),
         "vg_eefk_device": ([ctypes.c_char_p, _p, _sz, _p, _p], _i),
@@ -122,6 +124,8 @@ EXPORTED = (
     "vg_env_add_heightfield",
     "vg_validate_vectors_device",
     "vg_validate_vectors",
+    "vg_filter_self_from_pointcloud_device",
+    "vg_filter_self_from_pointcloud",
     "vg_env_attach",
     "vg_env_detach",
     "vg_eefk_device",

@@ -234,6 +234,29 @@ class Robot:
             return False
         return bool(self.validate_motion_batch(a, b, environment, resolution)[0])
 
+    def filter_self_from_pointcloud(self, pc, point_radius: float, configuration, environment: Environment | None = None):
+        """The points of pc (spheres of point_radius) that collide neither with the robot at
+        `configuration` nor with the environment, in order (bindings/robot_helper.hh:307-345).
+        pc: host array [n, 3] (returns an array) or CUDA tensor (returns a tensor)."""
+        env = environment if environment is not None else Environment()
+        q = np.ascontiguousarray(configuration, np.float32).reshape(self._dim)
+        m = ctypes.c_size_t()
+        if _is_cuda_tensor(pc):
+            import torch
+
+            pts = pc.detach().to(torch.float32).reshape(-1, 3).contiguous()
+            out = torch.empty_like(pts)
+            with torch.cuda.device(pts.device):
+                check(lib.vg_filter_self_from_pointcloud_device(self._b, env.handle, pts.data_ptr(), pts.shape[0],
+                                                                float(point_radius), _ptr(q), out.data_ptr(),
+                                                                ctypes.byref(m), _stream(pts)))
+            return out[: m.value]
+        pts = np.ascontiguousarray(pc, np.float32).reshape(-1, 3)
+        out = np.zeros_like(pts)
+        check(lib.vg_filter_self_from_pointcloud(self._b, env.handle, _ptr(pts), len(pts), float(point_radius), _ptr(q),
+                                                 _ptr(out), ctypes.byref(m)))
+        return out[: m.value].copy()
+
     def eefk(self, configuration) -> np.ndarray:
         """End-effector transform, a row-major 4x4 float32 matrix (Robot::eefk; binding
         robot_helper.hh:302-305)."""

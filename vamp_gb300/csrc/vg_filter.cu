@@ -744,6 +744,35 @@ namespace vg
             return VG_OK;
         }
 
+        // filter_self_from_pointcloud (bindings/robot_helper.hh:307-345): flags[i] = point i (a
+        // sphere of `radius`) collides with no fine sphere of the robot and no environment object.
+        // A warp-uniform loop: the environment query takes votes over the whole warp.
+        __global__ void filter_self_kernel(const float *xyz, long long n, float radius, const float *spheres, int fine,
+                                           EnvDevice env, uint32_t *flags)
+        {
+            extern __shared__ float4 smem[];
+            const EnvView ev = stage_env(env, smem);
+            const int lane = threadIdx.x & 31;
+            const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+            for (long long b = static_cast<long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); b < n; b += stride)
+            {
+                const long long i = b + lane;
+                const bool in = i < n;
+                const float x = in ? xyz[3 * i] : 0.0f, y = in ? xyz[3 * i + 1] : 0.0f, z = in ? xyz[3 * i + 2] : 0.0f;
+                bool valid = in;
+                for (int k = 0; k < fine; ++k)
+                {
+                    // sphere_sphere_sql2(robot sphere, point) < 0, scalar
+                    const float dx = __fsub_rn(__ldg(spheres + 4 * k), x), dy = __fsub_rn(__ldg(spheres + 4 * k + 1), y);
+                    const float dz = __fsub_rn(__ldg(spheres + 4 * k + 2), z), rs = __fadd_rn(__ldg(spheres + 4 * k + 3), radius);
+                    valid &= !(__fsub_rn(__fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy))), __fmul_rn(rs, rs)) < 0.0f);
+                }
+                const unsigned hit = env_query<1>(ev, x, y, z, radius, __ballot_sync(kFull, valid));
+                if (in)
+                    flags[i] = valid && !((hit >> lane) & 1u) ? 1u : 0u;
+            }
+        }
+
         int check_filter_args(const float *xyz, size_t n, const float *origin, const float *wmin, const float *wmax,
                               const float *out, const size_t *n_out)
         {
@@ -771,6 +800,75 @@ int vg_filter_pointcloud_device(const float *xyz, size_t n, float min_dist, floa
         return VG_OK;
     return filter_on_device(xyz, n, min_dist, max_range, origin, workcell_min, workcell_max, cull, out, n_out,
                             static_cast<cudaStream_t>(stream));
+}
+
+int vg_filter_self_from_pointcloud_device(const char *robot, vg_env *env, const float *xyz, size_t n, float point_radius,
+                                          const float *q, float *out, size_t *n_out, void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || !q || !n_out || (n && (!xyz || !out)))
+        return set_error(VG_ERR_ARG, "vg_filter_self_from_pointcloud: bad argument");
+    if (n > (size_t{1} << 31) - 1)
+        return set_error(VG_ERR_LIMIT, "vg_filter_self_from_pointcloud: at most 2^31 - 1 points");
+    *n_out = 0;
+    if (n == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const long long N = static_cast<long long>(n), tiles = blocks_of(N, kTile);
+    FilterBuffers fb;
+    float *dq = fb.get<float>(r->dim), *sph = fb.get<float>(4 * r->slots);
+    uint32_t *flags = fb.get<uint32_t>(N), *sums = fb.get<uint32_t>(tiles), *offs = fb.get<uint32_t>(tiles + 1);
+    uint32_t *idx = fb.get<uint32_t>(N);
+    if (fb.err != cudaSuccess)
+        return cuda_fail(fb.err, "vg_filter_self_from_pointcloud: cudaMalloc");
+    VG_CUDA(cudaMemcpyAsync(dq, q, r->dim * sizeof(float), cudaMemcpyHostToDevice, s), "vg_filter_self_from_pointcloud: copy");
+    VG_CUDA(r->spheres(dq, 1, sph, s), "vg_filter_self_from_pointcloud: sphere_fk");
+    const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4));
+    int occ = 0;
+    if (int rc = prepare_kernel(reinterpret_cast<const void *>(&filter_self_kernel), smem, 256, &occ))
+        return rc;
+    const int grid = static_cast<int>(std::min<long long>(blocks_of(N, 256), static_cast<long long>(sm_count()) * occ));
+    filter_self_kernel<<<grid, 256, smem, s>>>(xyz, N, point_radius, sph, r->fine, env_device(env), flags);
+    tile_sums<<<static_cast<unsigned>(tiles), kTile, 0, s>>>(flags, N, sums);
+    scan_tiles<<<1, kTile, 0, s>>>(sums, tiles, offs);
+    compact<<<static_cast<unsigned>(tiles), kTile, 0, s>>>(flags, N, offs, nullptr, idx);
+    VG_CUDA(cudaGetLastError(), "vg_filter_self_from_pointcloud: launch");
+    uint32_t m = 0;
+    VG_CUDA(cudaMemcpyAsync(&m, offs + tiles, sizeof(m), cudaMemcpyDeviceToHost, s), "vg_filter_self_from_pointcloud: copy");
+    VG_CUDA(cudaStreamSynchronize(s), "vg_filter_self_from_pointcloud");
+    if (m > 0)
+    {
+        gather_points<<<blocks_of(m, 256), 256, 0, s>>>(xyz, idx, m, out);
+        VG_CUDA(cudaGetLastError(), "vg_filter_self_from_pointcloud: launch");
+        VG_CUDA(cudaStreamSynchronize(s), "vg_filter_self_from_pointcloud");
+    }
+    *n_out = m;
+    return VG_OK;
+}
+
+int vg_filter_self_from_pointcloud(const char *robot, vg_env *env, const float *xyz, size_t n, float point_radius,
+                                   const float *q, float *out, size_t *n_out)
+{
+    if (!n_out || (n && (!xyz || !out)))
+        return set_error(VG_ERR_ARG, "vg_filter_self_from_pointcloud: bad argument");
+    *n_out = 0;
+    if (n == 0)
+        return VG_OK;
+    float *d_in = nullptr;
+    VG_CUDA(cudaMalloc(&d_in, 2 * n * 3 * sizeof(float)), "vg_filter_self_from_pointcloud: cudaMalloc");
+    float *d_out = d_in + 3 * n;
+    int rc = VG_OK;
+    cudaError_t e = cudaMemcpy(d_in, xyz, n * 3 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        rc = vg_filter_self_from_pointcloud_device(robot, env, d_in, n, point_radius, q, d_out, n_out, nullptr);
+    if (e == cudaSuccess && rc == VG_OK && *n_out)
+        e = cudaMemcpy(out, d_out, *n_out * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "vg_filter_self_from_pointcloud: copy");
+    return rc;
 }
 
 int vg_filter_pointcloud(const float *xyz, size_t n, float min_dist, float max_range, const float *origin,
