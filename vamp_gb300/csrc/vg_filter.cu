@@ -5,7 +5,8 @@
 // Morton code and drops every entry within min_dist of the last entry kept.  Here each pass is:
 //   1. codes: one 64-bit key per entry, (Morton code << 32) | position, so that sorting the keys
 //      is the stable sort by code; the coordinate range of the next pass is reduced on the side;
-//   2. a bitonic sort of the keys (shared-memory tiles of 2048 for the short strides);
+//   2. a sort of the keys: a stable radix sort on the code for long lists, a bitonic network
+//      (shared-memory tiles of 2048 for the short strides) for short ones;
 //   3. next[j]: the first entry after j that is farther than min_dist from entry j, found by a
 //      forward scan that skips 32-, 1024- and 32768-entry tiles whose bounding box lies inside
 //      the min_dist ball (tested in double with a margin, so a skipped entry is never "far");
@@ -33,6 +34,7 @@ namespace vg
         constexpr int kTile = 1024;      // entries per scan tile and per chain chunk
         constexpr int kSortTile = 2048;  // entries per shared-memory bitonic tile
         constexpr int kCodeBlock = 256;
+        constexpr long long kRadixMin = 16384;  // lists longer than this are radix-sorted
 
         __device__ __forceinline__ float sqdist(float ax, float ay, float az, float bx, float by, float bz)
         {
@@ -300,6 +302,65 @@ namespace vg
                 return;
             const long long i = 2 * t - (t & (j - 1));
             cmp_swap(keys[i], keys[i + j], (i & k) == 0);
+        }
+
+        // --- stable LSD radix sort of the keys by their upper 32 bits (the Morton code) ----------
+        //
+        // Four passes of 8 bits.  Per pass: per-tile digit counts, an exclusive scan over (digit,
+        // tile), and a stable scatter: an entry's rank among the equal digits of its tile is its
+        // rank in its warp (match + popcount) plus the counts of the earlier warps.  The keys
+        // enter in position order, so the result is the (code, position) order.
+
+        constexpr int kRadixTile = 1024;
+
+        __global__ void radix_count(const unsigned long long *keys, long long m, int shift, uint32_t *counts, long long tiles)
+        {
+            __shared__ uint32_t h[256];
+            for (int d = threadIdx.x; d < 256; d += blockDim.x)
+                h[d] = 0u;
+            __syncthreads();
+            const long long i = static_cast<long long>(blockIdx.x) * kRadixTile + threadIdx.x;
+            if (i < m)
+                atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+            __syncthreads();
+            for (int d = threadIdx.x; d < 256; d += blockDim.x)
+                counts[static_cast<long long>(d) * tiles + blockIdx.x] = h[d];
+        }
+
+        // out[i] = chunk_offs[chunk] + exclusive scan of values within its 1024-value chunk
+        __global__ void scan_apply(const uint32_t *values, long long n, const uint32_t *chunk_offs, uint32_t *out)
+        {
+            const long long i = static_cast<long long>(blockIdx.x) * kTile + threadIdx.x;
+            uint32_t total;
+            const uint32_t at = block_scan(i < n ? values[i] : 0u, &total);
+            if (i < n)
+                out[i] = chunk_offs[blockIdx.x] + at;
+        }
+
+        __global__ void radix_scatter(const unsigned long long *in, long long m, int shift, const uint32_t *offs, long long tiles,
+                                      unsigned long long *out)
+        {
+            __shared__ uint32_t wc[kRadixTile / 32][256];
+            const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+            for (int k = t; k < (kRadixTile / 32) * 256; k += blockDim.x)
+                (&wc[0][0])[k] = 0u;
+            __syncthreads();
+            const long long i = static_cast<long long>(blockIdx.x) * kRadixTile + t;
+            const bool valid = i < m;
+            const unsigned long long key = valid ? in[i] : 0ull;
+            const unsigned d = valid ? static_cast<unsigned>((key >> shift) & 255u) : 256u;
+            const unsigned peers = __match_any_sync(kFull, d);
+            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+            if (valid && rank == 0)
+                wc[w][d] = __popc(peers);
+            __syncthreads();
+            if (valid)
+            {
+                uint32_t base = 0;
+                for (int k = 0; k < w; ++k)
+                    base += wc[k][d];
+                out[offs[static_cast<long long>(d) * tiles + blockIdx.x] + base + rank] = key;
+            }
         }
 
         // the sorted entries' point indices and coordinates
@@ -639,7 +700,10 @@ namespace vg
             uint32_t *sidx = fb.get<uint32_t>(N + 1), *next = fb.get<uint32_t>(N + 1), *exit_of = fb.get<uint32_t>(N + 1);
             uint32_t *entry = fb.get<uint32_t>(tiles);
             uint32_t *exit_super = fb.get<uint32_t>(N + 1), *entry_super = fb.get<uint32_t>(blocks_of(tiles, kSuper));
-            unsigned long long *keys = fb.get<unsigned long long>(M);
+            unsigned long long *keys = fb.get<unsigned long long>(M), *keys2 = fb.get<unsigned long long>(N + 1);
+            const long long rtiles = blocks_of(N + 1, kRadixTile), rchunks = blocks_of(256 * rtiles, kTile);
+            uint32_t *rcount = fb.get<uint32_t>(256 * rtiles), *rstart = fb.get<uint32_t>(256 * rtiles);
+            uint32_t *rsums = fb.get<uint32_t>(rchunks), *roffs = fb.get<uint32_t>(rchunks + 1);
             float4 *sp = fb.get<float4>(N + 1);
             Box *b32 = fb.get<Box>(blocks_of(N + 1, 32)), *b1k = fb.get<Box>(blocks_of(N + 1, 1024)),
                 *b32k = fb.get<Box>(blocks_of(N + 1, 32768));
@@ -694,7 +758,23 @@ namespace vg
                 codes_kernel<<<static_cast<unsigned>(cb), kCodeBlock, 0, s>>>(xyz, list, m, Mp, perms[pass][0], perms[pass][1],
                                                                              perms[pass][2], range, keys, part_lo, part_hi);
                 range_kernel<<<1, 1024, 0, s>>>(part_lo, part_hi, cb, range);
-                if (Mp > 1)
+                if (m > kRadixMin)
+                {
+                    // large lists: the radix sort (digit counts, their scan, stable scatters)
+                    const long long rt = blocks_of(m, kRadixTile), nc = 256 * rt, cchunks = blocks_of(nc, kTile);
+                    unsigned long long *src = keys, *dst = keys2;
+                    for (int shift = 32; shift < 64; shift += 8)
+                    {
+                        radix_count<<<static_cast<unsigned>(rt), kRadixTile, 0, s>>>(src, m, shift, rcount, rt);
+                        tile_sums<<<static_cast<unsigned>(cchunks), kTile, 0, s>>>(rcount, nc, rsums);
+                        scan_tiles<<<1, kTile, 0, s>>>(rsums, cchunks, roffs);
+                        scan_apply<<<static_cast<unsigned>(cchunks), kTile, 0, s>>>(rcount, nc, roffs, rstart);
+                        radix_scatter<<<static_cast<unsigned>(rt), kRadixTile, 0, s>>>(src, m, shift, rstart, rt, dst);
+                        std::swap(src, dst);
+                    }
+                    // four passes: the result is back in keys
+                }
+                else if (Mp > 1)
                 {
                     const long long T = std::min<long long>(Mp, kSortTile);
                     const unsigned tb = static_cast<unsigned>(Mp / T), tt = static_cast<unsigned>(T / 2);
