@@ -662,26 +662,35 @@ namespace vg
         }
 
         // device buffers of one filter call
+        // device buffers of one filter call, carved out of one allocation: a first round of get()
+        // calls measures, allocate() reserves the total, a second round hands out the pointers
         struct FilterBuffers
         {
-            std::vector<void *> owned;
+            char *base = nullptr;
+            size_t used = 0;
+            bool measuring = true;
             cudaError_t err = cudaSuccess;
 
             template <typename T>
             T *get(size_t count)
             {
-                void *p = nullptr;
-                if (err == cudaSuccess)
-                    err = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-                if (err == cudaSuccess)
-                    owned.push_back(p);
-                return static_cast<T *>(p);
+                const size_t bytes = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+                const size_t at = used;
+                used += bytes;
+                return measuring ? nullptr : reinterpret_cast<T *>(base + at);
+            }
+
+            void allocate()
+            {
+                err = cudaMalloc(&base, used);
+                used = 0;
+                measuring = false;
             }
 
             ~FilterBuffers()
             {
-                for (void *p : owned)
-                    cudaFree(p);
+                if (base)
+                    cudaFree(base);
             }
         };
 
@@ -695,24 +704,47 @@ namespace vg
                 M <<= 1;
             const long long tiles = blocks_of(N + 1, kTile);
             FilterBuffers fb;
-            uint32_t *flags = fb.get<uint32_t>(N + 1), *list = fb.get<uint32_t>(N + 1), *list2 = fb.get<uint32_t>(N + 1);
-            uint32_t *sums = fb.get<uint32_t>(tiles), *offs = fb.get<uint32_t>(tiles + 1);
-            uint32_t *sidx = fb.get<uint32_t>(N + 1), *next = fb.get<uint32_t>(N + 1), *exit_of = fb.get<uint32_t>(N + 1);
-            uint32_t *entry = fb.get<uint32_t>(tiles);
-            uint32_t *exit_super = fb.get<uint32_t>(N + 1), *entry_super = fb.get<uint32_t>(blocks_of(tiles, kSuper));
-            unsigned long long *keys = fb.get<unsigned long long>(M), *keys2 = fb.get<unsigned long long>(N + 1);
+            uint32_t *flags, *list, *list2, *sums, *offs, *sidx, *next, *exit_of, *entry, *exit_super, *entry_super;
+            uint32_t *rcount, *rstart, *rsums, *roffs, *err;
+            unsigned long long *keys, *keys2;
+            float4 *sp;
+            Box *b32, *b1k, *b32k;
+            float *part_lo, *part_hi;
+            Range *range;
             const long long rtiles = blocks_of(N + 1, kRadixTile), rchunks = blocks_of(256 * rtiles, kTile);
-            uint32_t *rcount = fb.get<uint32_t>(256 * rtiles), *rstart = fb.get<uint32_t>(256 * rtiles);
-            uint32_t *rsums = fb.get<uint32_t>(rchunks), *roffs = fb.get<uint32_t>(rchunks + 1);
-            float4 *sp = fb.get<float4>(N + 1);
-            Box *b32 = fb.get<Box>(blocks_of(N + 1, 32)), *b1k = fb.get<Box>(blocks_of(N + 1, 1024)),
-                *b32k = fb.get<Box>(blocks_of(N + 1, 32768));
             const long long code_blocks = blocks_of(M, kCodeBlock);
-            float *part_lo = fb.get<float>(code_blocks), *part_hi = fb.get<float>(code_blocks);
-            Range *range = fb.get<Range>(1);
-            uint32_t *err = fb.get<uint32_t>(1);
+            auto carve = [&]() {
+                flags = fb.get<uint32_t>(N + 1);
+                list = fb.get<uint32_t>(N + 1);
+                list2 = fb.get<uint32_t>(N + 1);
+                sums = fb.get<uint32_t>(tiles);
+                offs = fb.get<uint32_t>(tiles + 1);
+                sidx = fb.get<uint32_t>(N + 1);
+                next = fb.get<uint32_t>(N + 1);
+                exit_of = fb.get<uint32_t>(N + 1);
+                entry = fb.get<uint32_t>(tiles);
+                exit_super = fb.get<uint32_t>(N + 1);
+                entry_super = fb.get<uint32_t>(blocks_of(tiles, kSuper));
+                keys = fb.get<unsigned long long>(M);
+                keys2 = fb.get<unsigned long long>(N + 1);
+                rcount = fb.get<uint32_t>(256 * rtiles);
+                rstart = fb.get<uint32_t>(256 * rtiles);
+                rsums = fb.get<uint32_t>(rchunks);
+                roffs = fb.get<uint32_t>(rchunks + 1);
+                sp = fb.get<float4>(N + 1);
+                b32 = fb.get<Box>(blocks_of(N + 1, 32));
+                b1k = fb.get<Box>(blocks_of(N + 1, 1024));
+                b32k = fb.get<Box>(blocks_of(N + 1, 32768));
+                part_lo = fb.get<float>(code_blocks);
+                part_hi = fb.get<float>(code_blocks);
+                range = fb.get<Range>(1);
+                err = fb.get<uint32_t>(1);
+            };
+            carve();
+            fb.allocate();
             if (fb.err != cudaSuccess)
                 return cuda_fail(fb.err, "vg_filter_pointcloud: cudaMalloc");
+            carve();
 
             const float sq = min_dist * min_dist, sq_range = max_range * max_range;
             // collision/filter.hh:194-197: both ends are minima over the axes
@@ -898,11 +930,21 @@ int vg_filter_self_from_pointcloud_device(const char *robot, vg_env *env, const 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const long long N = static_cast<long long>(n), tiles = blocks_of(N, kTile);
     FilterBuffers fb;
-    float *dq = fb.get<float>(r->dim), *sph = fb.get<float>(4 * r->slots);
-    uint32_t *flags = fb.get<uint32_t>(N), *sums = fb.get<uint32_t>(tiles), *offs = fb.get<uint32_t>(tiles + 1);
-    uint32_t *idx = fb.get<uint32_t>(N);
+    float *dq, *sph;
+    uint32_t *flags, *sums, *offs, *idx;
+    auto carve = [&]() {
+        dq = fb.get<float>(r->dim);
+        sph = fb.get<float>(4 * r->slots);
+        flags = fb.get<uint32_t>(N);
+        sums = fb.get<uint32_t>(tiles);
+        offs = fb.get<uint32_t>(tiles + 1);
+        idx = fb.get<uint32_t>(N);
+    };
+    carve();
+    fb.allocate();
     if (fb.err != cudaSuccess)
         return cuda_fail(fb.err, "vg_filter_self_from_pointcloud: cudaMalloc");
+    carve();
     VG_CUDA(cudaMemcpyAsync(dq, q, r->dim * sizeof(float), cudaMemcpyHostToDevice, s), "vg_filter_self_from_pointcloud: copy");
     VG_CUDA(r->spheres(dq, 1, sph, s), "vg_filter_self_from_pointcloud: sphere_fk");
     const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4));
