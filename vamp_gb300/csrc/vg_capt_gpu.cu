@@ -16,6 +16,7 @@
 #include "vg_internal.h"
 
 #include <algorithm>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -540,22 +541,39 @@ namespace vg
         NodeInfo *info = nullptr;
         size_t items_cap = 0, child_cap = 0;
         cudaError_t e = cudaSuccess;
+        // the fixed-size scratch in one allocation (carved in 256-byte aligned pieces)
+        char *scratch = nullptr;
+        {
+            size_t used = 0;
+            auto carve = [&](auto **p, size_t count) {
+                const size_t at = used;
+                used += (std::max<size_t>(count, 1) * sizeof(**p) + 255) & ~size_t(255);
+                *p = scratch ? reinterpret_cast<std::remove_reference_t<decltype(*p)>>(scratch + at) : nullptr;
+            };
+            auto carve_all = [&]() {
+                used = 0;
+                carve(&px, N);
+                carve(&py, N);
+                carve(&pz, N);
+                carve(&key, N);
+                carve(&ord, N);
+                carve(&pos, N);
+                carve(&cell, 6 * N);
+                carve(&child_cell, 6 * N);
+                carve(&off, N + 1);
+                carve(&child_off, N + 1);
+                carve(&sizes, N);
+                carve(&info, N / 2 > 0 ? N / 2 : 1);
+            };
+            carve_all();
+            e = cudaMalloc(&scratch, used);
+            if (e == cudaSuccess)
+                carve_all();
+        }
         auto alloc = [&](auto **p, size_t count) {
             if (e == cudaSuccess)
                 e = cudaMalloc(p, std::max<size_t>(count, 1) * sizeof(**p));
         };
-        alloc(&px, N);
-        alloc(&py, N);
-        alloc(&pz, N);
-        alloc(&key, N);
-        alloc(&ord, N);
-        alloc(&pos, N);
-        alloc(&cell, 6 * N);
-        alloc(&child_cell, 6 * N);
-        alloc(&off, N + 1);
-        alloc(&child_off, N + 1);
-        alloc(&sizes, N);
-        alloc(&info, N / 2 > 0 ? N / 2 : 1);
         alloc(&out.tests, N - 1);
         alloc(&out.aabbs, 6 * N);
         alloc(&out.starts_dev, N + 1);
@@ -642,11 +660,7 @@ namespace vg
             out.starts_dev = nullptr;
             out.top_dev = nullptr;
         }
-        for (void *p : {static_cast<void *>(px), static_cast<void *>(py), static_cast<void *>(pz), static_cast<void *>(key),
-                        static_cast<void *>(cell), static_cast<void *>(child_cell), static_cast<void *>(ord),
-                        static_cast<void *>(pos), static_cast<void *>(items), static_cast<void *>(child_items),
-                        static_cast<void *>(off), static_cast<void *>(child_off), static_cast<void *>(sizes),
-                        static_cast<void *>(info)})
+        for (void *p : {static_cast<void *>(scratch), static_cast<void *>(items), static_cast<void *>(child_items)})
         {
             if (p)
                 cudaFree(p);
