@@ -11,7 +11,7 @@ no counterpart in the reference, `autotune`, `Batch` (checks replayed as one CUD
 
 The CUDA library is loaded on first use of any of those names; if it has not been built the
 access raises ImportError (there is no CPU fallback).  Submodules that do not need the GPU
-(build, scenes, robots, robotgen) import without it.
+(build, scenes, robots, robotgen, factory, roadmap) import without it.
 """
 from __future__ import annotations
 

@@ -106,10 +106,15 @@ class Environment:
             env.attach(a)
         return env
 
-    def add_pointcloud(self, points, r_min: float, r_max: float, r_point: float) -> None:
-        """A pointcloud checked as a CAPT (collision/capt.hh), built on the host."""
+    def add_pointcloud(self, points, r_min: float, r_max: float, r_point: float) -> int:
+        """A pointcloud checked as a CAPT (collision/capt.hh), built on the host.  Returns the build
+        time in nanoseconds, as the reference's binding does (bindings/environment.cc:150-161)."""
+        import time
+
         pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        t0 = time.perf_counter_ns()
         check(lib.vg_env_add_pointcloud(self._h, _ptr(pts), len(pts), float(r_min), float(r_max), float(r_point)))
+        return time.perf_counter_ns() - t0
 
     def add_pointcloud_device(self, points, r_min: float, r_max: float, r_point: float) -> None:
         """The same CAPT built on the GPU from a CUDA tensor of points [n, 3] (float32); the layout
