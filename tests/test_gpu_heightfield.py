@@ -96,3 +96,35 @@ def test_heightfield_api(vg):
     env.add_heightfield(hf)
     with pytest.raises(ValueError):
         env.add_heightfield(vg.make_heightfield((0, 0, 0), (1, 1, 1), (3, 3), np.zeros(8)))
+
+
+def test_batch_graph_with_extended_environments(vg, port):
+    """A CUDA-graph batch mixing an environment with a heightfield and an attachment and a plain
+    one: replays give the single checks' (and the oracle's) verdicts."""
+    import torch
+
+    from vamp_gb300 import scenes
+
+    tf = np.eye(4, dtype=np.float32)
+    tf[2, 3] = 0.1
+    ext = _scene(scenes.heightfield(21), scenes.scene_config1(22))
+    ext["attachment"] = {"tf": tf, "spheres": np.array([[0, 0, 0, 0.05]], np.float32)}
+    plain = scenes.scene_config1(23)
+    parts = [("panda", ext), ("ur5", plain)]
+    b = vg.Batch()
+    keep = []
+    for name, scene in parts:
+        prb = port.robot(name)
+        a, bb = scenes.edges(prb.s_m, prb.s_a, 1024, 24)
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(bb).cuda()
+        out = torch.zeros(len(a), dtype=torch.uint8, device="cuda")
+        env = vg.Environment.from_scene(scene)
+        b.add(getattr(vg, name), env, da, db, out)
+        keep.append((name, scene, a, bb, out, env))
+    for _ in range(2):  # capture, then replay
+        b.launch()
+        torch.cuda.synchronize()
+        for name, scene, a, bb, out, env in keep:
+            prb = port.robot(name)
+            want, _ = port.env(scene).validate_motions(prb, a, bb, prb.resolution, threads=THREADS)
+            assert np.array_equal(out.cpu().numpy(), want), name
