@@ -167,8 +167,8 @@ namespace vg
 
     // Uploads each pointcloud's tree once: kCloudBuffers device buffers per cloud (tests, aabbs,
     // starts, the reference-layout blocks, the ring-ordered blocks the queries scan, and the
-    // blocks' ring bounds).  A host-built cloud's reference-layout blocks are freed once ordered
-    // (the host copy answers layout queries).
+    // query tables).  A host-built cloud's reference-layout blocks are freed once ordered (the
+    // host copy answers layout queries).
     static int upload_clouds(vg_env *e)
     {
         while (e->d_clouds.size() < kCloudBuffers * e->clouds.size())
@@ -195,9 +195,10 @@ namespace vg
                     return cuda_fail(err, "upload pointcloud");
                 }
             }
-            float *aff_q = nullptr, *ring_lo = nullptr;
-            const int rc = capt_ring_order(static_cast<const float *>(dst[0]), c.nlog2, static_cast<const uint32_t *>(dst[2]),
-                                           static_cast<const float *>(dst[3]), c.blocks(), c.r_max, c.r_point, &aff_q, &ring_lo);
+            CaptQuery q;
+            const int rc = capt_query_layout(static_cast<const float *>(dst[0]), c.nlog2, static_cast<const float *>(dst[1]),
+                                             static_cast<const uint32_t *>(dst[2]), static_cast<const float *>(dst[3]), c.blocks(),
+                                             c.r_max, c.r_point, q);
             cudaFree(dst[3]);
             dst[3] = nullptr;
             if (rc != VG_OK)
@@ -210,8 +211,9 @@ namespace vg
             {
                 e->d_clouds.push_back(dst[k]);
             }
-            e->d_clouds.push_back(aff_q);
-            e->d_clouds.push_back(ring_lo);
+            e->d_clouds.push_back(q.aff_q);
+            e->d_clouds.push_back(q.tables);
+            e->capt_q.push_back(q);
         }
         return VG_OK;
     }
@@ -223,17 +225,21 @@ namespace vg
         {
             const CaptHost &c = e->clouds[i];
             CaptView v{};
-            void *const *d = &e->d_clouds[kCloudBuffers * i];
-            v.tests = static_cast<const float *>(d[0]);
-            v.aabbs = static_cast<const float *>(d[1]);
-            v.starts = static_cast<const uint32_t *>(d[2]);
-            v.aff = static_cast<const float4 *>(d[4]);  // ring order
-            v.ring_lo = static_cast<const float *>(d[5]);
+            const CaptQuery &q = e->capt_q[i];
+            v.nodes = q.nodes;
+            v.leaves = q.leaves;
+            v.ends = q.ends;
+            v.aff = reinterpret_cast<const float4 *>(q.aff_q);
             for (int k = 0; k < 6; ++k)
                 v.top[k] = c.top[k];
             v.r_point = c.r_point;
             v.nlog2 = c.nlog2;
-            v.n_tests = static_cast<int>(c.n_tests());
+            for (int k = 0; k < 3; ++k)
+                v.top_tests[k] = q.top_tests[k];
+            v.rem = q.rem;
+            v.groups = q.groups;
+            for (int k = 0; k < kCaptRings; ++k)
+                v.ring_edge[k] = q.ring_edge[k];
             const size_t at = img.size();
             img.resize(at + sizeof(CaptView) / sizeof(float4));
             std::memcpy(&img[at], &v, sizeof(CaptView));
@@ -620,8 +626,8 @@ int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float 
     DeviceCapt d;
     if (int rc = capt_build_device(xyz, n, r_min, r_max, r_point, static_cast<cudaStream_t>(stream), d))
         return rc;
-    float *aff_q = nullptr, *ring_lo = nullptr;
-    if (int rc = capt_ring_order(d.tests, d.nlog2, d.starts, d.aff, d.blocks, r_max, r_point, &aff_q, &ring_lo))
+    CaptQuery q;
+    if (int rc = capt_query_layout(d.tests, d.nlog2, d.aabbs, d.starts, d.aff, d.blocks, r_max, r_point, q))
     {
         d.release();
         return rc;
@@ -639,8 +645,9 @@ int vg_env_add_pointcloud_device(vg_env *env, const float *xyz, size_t n, float 
     env->d_clouds.push_back(d.aabbs);
     env->d_clouds.push_back(d.starts);
     env->d_clouds.push_back(d.aff);  // reference layout, kept for vg_env_pointcloud_layout
-    env->d_clouds.push_back(aff_q);
-    env->d_clouds.push_back(ring_lo);
+    env->d_clouds.push_back(q.aff_q);
+    env->d_clouds.push_back(q.tables);
+    env->capt_q.push_back(q);
     env->device = dev;
     env->dirty = true;
     return VG_OK;

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include "vg_check.cuh"
+
 #include <cstddef>
 #include <cstdint>
 
@@ -30,10 +32,22 @@ namespace vg
     int capt_build_device(const float *xyz, size_t n, float r_min, float r_max, float r_point, cudaStream_t s,
                           DeviceCapt &out);
 
-    // The query order of a tree's affordance lists (vg_capt_ring.cu): each leaf's points
-    // regrouped by distance to the leaf's cell, nearest ring first (aff_q, blocks x 24), and per
-    // block the lower edge of its first point's ring (ring_lo, non-decreasing within a leaf).
-    // Allocates both; synchronous.
-    int capt_ring_order(const float *tests, int nlog2, const uint32_t *starts, const float *aff, size_t blocks,
-                        float r_max, float r_point, float **aff_q, float **ring_lo);
+    // The tables a CAPT query reads on the device (vg_capt_ring.cu).  aff_q and tables are owned
+    // by the caller once built (cudaFree each); nodes, leaves and ends point into tables.
+    struct CaptQuery
+    {
+        float *aff_q = nullptr;     // blocks x 24: each leaf's points, nearest ring first
+        void *tables = nullptr;     // one allocation holding the three tables below
+        float4 *nodes = nullptr;    // split values three levels per node: 2 float4 per node
+        float4 *leaves = nullptr;   // per leaf: lower xyz, upper x | upper yz, first block (bits), 0
+        uint32_t *ends = nullptr;   // per leaf x kCaptRings: end of the blocks of ring r or nearer
+        float top_tests[3] = {0, 0, 0};  // split values of the nlog2 mod 3 levels above the groups
+        int rem = 0;                // nlog2 mod 3
+        int groups = 0;             // nlog2 / 3
+        float ring_edge[kCaptRings] = {};  // lower edge of ring r, rounded down
+    };
+
+    // Builds the query tables of a tree in device memory (its reference-layout arrays); synchronous.
+    int capt_query_layout(const float *tests, int nlog2, const float *aabbs, const uint32_t *starts, const float *aff,
+                          size_t blocks, float r_max, float r_point, CaptQuery &q);
 }  // namespace vg

@@ -167,22 +167,27 @@ namespace vg
         return kind == 0 ? 4 : (kind <= 2 ? 8 : 15);
     }
 
-    // One pointcloud's CAPT on the device (collision/capt.hh:584-617): split values, leaf boxes,
-    // per-leaf ranges of 8-point affordance blocks (x[8] y[8] z[8] = 6 float4 per block).
+    // One pointcloud's CAPT on the device: the query tables built from the reference layout
+    // (collision/capt.hh:584-617) by vg_capt_ring.cu.  Split values three tree levels per node
+    // (2 float4: the subtree's 7 values in heap order, then a pad) in groups of 2^rem * 8^g
+    // nodes; per leaf its box and first block (2 float4); per leaf and ring the end of the
+    // blocks up to that ring; the 8-point blocks (x[8] y[8] z[8] = 6 float4), each leaf's
+    // nearest ring first.
+    constexpr int kCaptRings = 32;
     struct CaptView
     {
-        const float *tests;
-        const float *aabbs;
-        const uint32_t *starts;
+        const float4 *nodes;
+        const float4 *leaves;
+        const uint32_t *ends;
         const float4 *aff;
         float top[6];
         float r_point;
         int nlog2;
-        int n_tests;
-        int pad;
-        // per affordance block, the lower edge of the distance ring of its first point (the
-        // blocks of aff are in ring order, nearest first; vg_capt_ring.cu)
-        const float *ring_lo;
+        float top_tests[3];  // the rem = nlog2 mod 3 levels above the first group, heap order
+        int rem;
+        int groups;          // nlog2 / 3
+        int pad[3];
+        float ring_edge[kCaptRings];  // lower edge of each distance ring, rounded down
     };
     constexpr int kMaxClouds = 4;
 
@@ -397,45 +402,62 @@ namespace vg
         {
             return;
         }
-        int idx = 0;
-        int k = 0;
-#pragma unroll 1
-        for (int i = 0; i < c.nlog2; ++i)
+        // the last ring whose lower edge is within the sphere's reach (the margin dwarfs the FP32
+        // error of the point test); independent of the descent
+        const float reach = fabsf(rad);
+        const float lim = __fmaf_rn(reach, 1e-5f, reach);
+        int ring = 0;
+#pragma unroll
+        for (int s = kCaptRings / 2; s > 0; s >>= 1)
         {
-            const float pk = k == 0 ? x : (k == 1 ? y : z);
-            idx = 2 * idx + 1 + (pk >= __ldg(c.tests + idx) ? 1 : 0);
-            k = k == 2 ? 0 : k + 1;
+            ring += c.ring_edge[ring + s] <= lim ? s : 0;
         }
-        const int leaf = idx - c.n_tests;
-        const float *box = c.aabbs + 6 * static_cast<long long>(leaf);
+        // descent (right child: coordinate >= split value; level i splits axis i mod 3): the
+        // levels above the first group one at a time, then three levels per node
+        uint32_t node = 0;
+        if (c.rem > 0)
+        {
+            const int r0 = x >= c.top_tests[0] ? 1 : 0;
+            node = r0;
+            if (c.rem > 1)
+            {
+                node = 2 * node + (y >= c.top_tests[1 + r0] ? 1 : 0);
+            }
+        }
+        const float q0 = c.rem == 0 ? x : (c.rem == 1 ? y : z);
+        const float q1 = c.rem == 0 ? y : (c.rem == 1 ? z : x);
+        const float q2 = c.rem == 0 ? z : (c.rem == 1 ? x : y);
+        const float4 *group = c.nodes;
+        uint32_t size = 1u << c.rem;
+#pragma unroll 1
+        for (int g = 0; g < c.groups; ++g)
+        {
+            const float4 t0 = __ldg(group + 2 * node), t1 = __ldg(group + 2 * node + 1);
+            const uint32_t c0 = q0 >= t0.x ? 1u : 0u;
+            const uint32_t c1 = q1 >= (c0 ? t0.z : t0.y) ? 1u : 0u;
+            const float t2 = c0 ? (c1 ? t1.z : t1.y) : (c1 ? t1.x : t0.w);
+            const uint32_t c2 = q2 >= t2 ? 1u : 0u;
+            node = 8u * node + 4u * c0 + 2u * c1 + c2;
+            group += 2 * static_cast<size_t>(size);
+            size *= 8u;
+        }
+        const float4 l0 = __ldg(c.leaves + 2 * static_cast<size_t>(node)), l1 = __ldg(c.leaves + 2 * static_cast<size_t>(node) + 1);
+        const uint32_t end = __ldg(c.ends + static_cast<size_t>(node) * kCaptRings + ring);
+        const float lo[3] = {l0.x, l0.y, l0.z}, hi[3] = {l0.w, l1.x, l1.y};
         float d[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j)
         {
-            const float lo = __ldg(box + j), hi = __ldg(box + 3 + j);
-            const float m = p[j] > lo ? p[j] : lo;
-            const float cl = m < hi ? m : hi;
+            const float m = p[j] > lo[j] ? p[j] : lo[j];
+            const float cl = m < hi[j] ? m : hi[j];
             d[j] = __fsub_rn(p[j], cl);
         }
         if (!(__fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmul_rn(d[0], d[0]))) <= rc))
         {
             return;
         }
-        b0 = __ldg(c.starts + leaf);
-        b1 = __ldg(c.starts + leaf + 1);
-        // the leaf's blocks come nearest ring first: drop those whose ring starts beyond the
-        // sphere's reach (the margin dwarfs the FP32 error of the point test)
-        const float lim = __fmaf_rn(rad, 1e-5f, rad);
-        uint32_t lo = b0, hi = b1;
-        while (lo < hi)
-        {
-            const uint32_t mid = lo + ((hi - lo) >> 1);
-            if (__ldg(c.ring_lo + mid) > lim)
-                hi = mid;
-            else
-                lo = mid + 1;
-        }
-        b1 = lo;
+        b0 = __float_as_uint(l1.z);
+        b1 = end;
     }
 
     // Whether any of the 8 points of affordance block b lies within sqrt(rc) of (x, y, z).
@@ -484,10 +506,11 @@ namespace vg
         bool hit = false;
         if (4u * longest <= VG_CAPT_SHARED_WEIGHT * shared_steps)
         {
+            // two blocks per step: their loads overlap
 #pragma unroll 1
-            for (uint32_t b = b0; b < b1 && !hit; ++b)
+            for (uint32_t b = b0; b < b1 && !hit; b += 2)
             {
-                hit = capt_block(c, b, x, y, z, rc);
+                hit = capt_block(c, b, x, y, z, rc) | (b + 1 < b1 && capt_block(c, b + 1, x, y, z, rc));
             }
         }
         else

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "vg_capt.h"
+#include "vg_capt_gpu.h"
 #include "vg_kernels.cuh"
 
 namespace vg
@@ -68,7 +69,7 @@ namespace vg
     } while (0)
 
     // device buffers per pointcloud: tests, aabbs, starts, reference-layout blocks (device-built
-    // clouds only), ring-ordered blocks, ring bounds
+    // clouds only), ring-ordered blocks, query tables
     constexpr size_t kCloudBuffers = 6;
 
     // threads per block of every checking kernel (the robots' stage stride)
@@ -115,9 +116,10 @@ struct vg_env
     // environments with heightfields or an attachment run the extended kernels
     bool extended() const { return n_att >= 0 || !hf.empty(); }
     int n[5] = {0, 0, 0, 0, 0};
-    // pointclouds: host trees and their device copies (tests, aabbs, starts, aff per cloud)
+    // pointclouds: host trees, their device buffers and the query tables built from them
     std::vector<vg::CaptHost> clouds;
-    std::vector<void *> d_clouds;  // kCloudBuffers buffers per uploaded cloud
+    std::vector<void *> d_clouds;        // kCloudBuffers buffers per uploaded cloud
+    std::vector<vg::CaptQuery> capt_q;   // per uploaded cloud (pointers into d_clouds)
     // library-owned scratch: work counter, staging for host-pointer calls
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;
