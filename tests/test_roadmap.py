@@ -9,7 +9,7 @@ import pytest
 
 torch = pytest.importorskip("torch")
 
-from vamp_gb300.roadmap import neighbour_pairs, prmstar_neighbors  # noqa: E402
+from vamp_gb300.roadmap import neighbour_pairs, prmstar_neighbors, prmstar_table  # noqa: E402
 
 
 def _incremental(nodes: np.ndarray, space: float, k_max=None, radius=None):
@@ -25,6 +25,13 @@ def _incremental(nodes: np.ndarray, space: float, k_max=None, radius=None):
             if d[j] <= r:
                 out.append((int(j), i))
     return out
+
+
+@pytest.mark.parametrize("dim", [6, 7, 14])
+def test_prmstar_table_is_the_per_node_form(dim):
+    ks, rs = prmstar_table(dim, 3.7, 0, 5000)
+    for i in range(5000):
+        assert (ks[i], rs[i]) == prmstar_neighbors(dim, 3.7, i), i
 
 
 def test_prmstar_parameters():

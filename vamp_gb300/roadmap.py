@@ -35,6 +35,18 @@ def prmstar_neighbors(dim: int, space_measure: float, num_states: int, gamma_sca
     return k, r
 
 
+def prmstar_table(dim: int, space_measure: float, i0: int, i1: int, gamma_scale: float = 2.0):
+    """prmstar_neighbors(dim, space_measure, i) for i in [i0, i1), as two lists: the same float
+    operations in the same order, with the terms that do not depend on i computed once."""
+    f = math.e + math.e / dim
+    ratio = space_measure / unit_ball_measure(dim)
+    c = 2.0 * (1.0 + 1.0 / dim) ** (1.0 / dim) * ratio ** (1.0 / dim)
+    inv = 1.0 / dim
+    ks = [int(math.ceil(f * math.log(i))) if i >= 2 else 0 for i in range(i0, i1)]
+    rs = [gamma_scale * c * (math.log(i) / i) ** inv if i >= 2 else 0.0 for i in range(i0, i1)]
+    return ks, rs
+
+
 def neighbour_pairs(nodes, space_measure: float, k_max: int | None = None, radius: float | None = None,
                     chunk: int = 4096):
     """Candidate edges (earlier node, node) of the incremental roadmap over `nodes` [n, dim] (a
@@ -53,11 +65,11 @@ def neighbour_pairs(nodes, space_measure: float, k_max: int | None = None, radiu
         idx = torch.arange(i0, i1, device=nodes.device)
         later = torch.arange(i1, device=nodes.device)[None, :] >= idx[:, None]  # self and later nodes
         d = d.masked_fill(later, float("inf"))
-        ks, rs = [], []
-        for i in range(i0, i1):
-            kk, rr = prmstar_neighbors(dim, space_measure, i)
-            ks.append(k_max if k_max is not None else kk)
-            rs.append(radius if radius is not None else rr)
+        ks, rs = prmstar_table(dim, space_measure, i0, i1)
+        if k_max is not None:
+            ks = [k_max] * (i1 - i0)
+        if radius is not None:
+            rs = [radius] * (i1 - i0)
         kmax = max(1, min(max(ks), i1))
         vals, order = torch.topk(d, kmax, dim=1, largest=False)
         kt = torch.tensor(ks, device=nodes.device)[:, None]
