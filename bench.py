@@ -86,6 +86,12 @@ def max_over_ranks(world, x: float) -> float:
     return float(t.item())
 
 
+def vg_schedules():
+    from vamp_gb300 import SCHEDULES
+
+    return SCHEDULES
+
+
 def workload():
     from vamp_gb300 import scenes
     from vamp_gb300.robots import model
@@ -245,7 +251,7 @@ def autotune(robot: str, env, a, b, resolution: int, stream, sample: int = 65536
     sched, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
     check(lib.vg_autotune_motions(robot.encode(), env.handle, a.data_ptr(), b.data_ptr(), min(sample, len(a)), resolution,
                                   ctypes.byref(sched), ctypes.byref(bps), ctypes.byref(ms), stream))
-    return {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][sched.value],
+    return {"schedule": vg_schedules()[sched.value],
             "blocks_per_sm": bps.value or "max", "sample_edges": min(sample, len(a)), "sample_ms": ms.value}
 
 
@@ -694,7 +700,7 @@ def run_gpu(args, world, rank, local):
         pick = autotune("panda", env, a, b, RESOLUTION, stream.cuda_stream)
     else:
         env.set_schedule(args.schedule)
-        pick = {"schedule": ["segment per edge", "warp per edge", "warp per edge, register-rich build"][args.schedule]}
+        pick = {"schedule": vg_schedules()[args.schedule]}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def launch():
@@ -792,7 +798,7 @@ def main():
     ap.add_argument("--labels", type=int, default=2 << 20, help="exact-checker labels the learned order trains on")
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
-                         "2 warp per edge with the register-rich build")
+                         "2 warp per edge with the register-rich build, 3 as 2 with free segments starting the next edge")
     ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug", "filter", "roadmap"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
                          "mixed: four robots in one CUDA graph; debug: per-sphere collision reports; "

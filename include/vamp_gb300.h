@@ -139,7 +139,8 @@ int vg_eefk(const char *robot, const float *q, size_t n, float *out);
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
 /* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):
  * 1 (default) = a warp checks consecutive blocks of one edge, 0 = each lane-block checks its own
- * edge, 2 = as 1 with the kernel built for fewer resident blocks and more registers per thread.
+ * edge, 2 = as 1 with the kernel built for fewer resident blocks and more registers per thread,
+ * 3 = as 2 with the segments an edge's last blocks leave free starting on the next edge.
  * No reference counterpart: the reference validates one edge at a time on one core. */
 int vg_env_set_schedule(vg_env *env, int schedule);
 /* Number of objects of a kind (0 spheres, 1 capsules, 2 z-capsules, 3 cuboids, 4 z-cuboids)
@@ -317,8 +318,9 @@ int vg_validate_motions_learned_device(
  *
  * vg_autotune_motions times the edge-check schedules on the given edges (device buffers, a
  * sample of the caller's workload) and keeps the fastest for this robot in env, where later edge
- * checks of that robot use it: a segment per edge (*schedule_out 0), a warp per edge (1), or a
- * warp per edge built for fewer resident blocks and more registers (2); and the resident
+ * checks of that robot use it: a segment per edge (*schedule_out 0), a warp per edge (1), a
+ * warp per edge built for fewer resident blocks and more registers (2), or the same with the
+ * segments an edge's last blocks leave free starting on the next edge (3); and the resident
  * blocks per SM (*blocks_per_sm_out, 0 = as many as fit); *ms_out is its time on the
  * sample.  Verdicts do not depend on the pick.  vg_env_set_schedule clears the picks.
  * Synchronous. */

@@ -190,7 +190,7 @@ def test_both_edge_schedules_agree_with_the_oracle(vg, port, torch, lanes, sqrt_
     a, b = scenes.edges(rb.s_m, rb.s_a, 8192, 88)
     cpu, cpu_blocks = port.env(scene, sqrt_mode=SQRT_X86 if sqrt_mode == 0 else SQRT_EXACT).validate_motions(
         rb, a, b, 32, lanes=lanes, threads=THREADS)
-    for schedule in (0, 1, 2):
+    for schedule in (0, 1, 2, 3):
         env = vg.Environment.from_scene(scene, lanes=lanes, sqrt_mode=sqrt_mode)
         env.set_schedule(schedule)
         blocks = torch.zeros(len(a), dtype=torch.int32, device="cuda")
@@ -198,6 +198,36 @@ def test_both_edge_schedules_agree_with_the_oracle(vg, port, torch, lanes, sqrt_
                                              blocks=blocks).cpu().numpy()
         assert np.array_equal(gpu, cpu), schedule
         assert np.array_equal(blocks.cpu().numpy(), cpu_blocks), schedule
+
+
+@pytest.mark.parametrize("lanes,sqrt_mode", [(8, 0), (4, 1)])
+def test_packed_schedule_with_short_and_mixed_edges(vg, port, torch, lanes, sqrt_mode):
+    """The packed schedule (free segments start the next edge) on edges of 1 to 12 blocks in
+    random order, so that most warp iterations hold the end of one edge and the start of the
+    next: the same verdicts and reference block counts as the oracle."""
+    from oracle.vgo import SQRT_EXACT, SQRT_X86
+    from vamp_gb300 import scenes
+
+    scene = scenes.scene_config1(9)
+    rb = port.robot("panda")
+    a, b = scenes.edges(rb.s_m, rb.s_a, 6144, 89)
+    rng = np.random.default_rng(90)
+    # edge lengths 0 .. 3 rad (1 to 12 blocks at resolution 32, 8 lanes), zero-length edges included
+    d = b - a
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    length = rng.uniform(0.0, 3.0, len(a)).astype(np.float32)
+    length[::97] = 0.0
+    b = (a + d * length[:, None]).astype(np.float32)
+    cpu, cpu_blocks = port.env(scene, sqrt_mode=SQRT_X86 if sqrt_mode == 0 else SQRT_EXACT).validate_motions(
+        rb, a, b, 32, lanes=lanes, threads=THREADS)
+    assert 0.05 < 1.0 - cpu.mean() < 0.95
+    env = vg.Environment.from_scene(scene, lanes=lanes, sqrt_mode=sqrt_mode)
+    env.set_schedule(3)
+    blocks = torch.zeros(len(a), dtype=torch.int32, device="cuda")
+    gpu = vg.panda.validate_motion_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), env, 32,
+                                         blocks=blocks).cpu().numpy()
+    assert np.array_equal(gpu, cpu)
+    assert np.array_equal(blocks.cpu().numpy(), cpu_blocks)
 
 
 def _cloud(points, r_min=0.012, r_max=0.08):

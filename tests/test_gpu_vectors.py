@@ -30,7 +30,7 @@ def test_vectors_match_the_reference(vg, robot):
 
 
 @pytest.mark.parametrize("robot", ["panda", "ur5", "fetch", "baxter"])
-@pytest.mark.parametrize("schedule", [0, 1, 2])
+@pytest.mark.parametrize("schedule", [0, 1, 2, 3])
 def test_vectors_are_the_oracles(vg, port, robot, schedule):
     import torch
 

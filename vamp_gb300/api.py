@@ -68,7 +68,9 @@ class Environment:
         self.lanes, self.sqrt_mode = lanes, sqrt_mode
 
     def set_schedule(self, schedule: int) -> None:
-        """GPU edge schedule: 1 (default) a warp per edge, 0 a lane-block per edge."""
+        """GPU edge schedule: 1 (default) a warp per edge, 0 a lane-block per edge, 2 a warp per
+        edge with the register-rich build, 3 as 2 with the segments an edge leaves free starting
+        on the next edge.  Verdicts and block counts are the same in every schedule."""
         check(lib.vg_env_set_schedule(self._h, schedule))
 
     def add_sphere(self, sphere) -> None:
@@ -396,7 +398,8 @@ baxter = Robot("baxter")
 # autotuner and learned-ordering entry points (include/vamp_gb300.h).  Device buffers are torch
 # CUDA tensors; calls run on the current stream.
 
-SCHEDULES = ("segment per edge", "warp per edge", "warp per edge, register-rich build")
+SCHEDULES = ("segment per edge", "warp per edge", "warp per edge, register-rich build",
+             "warp per edge, register-rich build, free segments start the next edge")
 
 
 def _stream(t):

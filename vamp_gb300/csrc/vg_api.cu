@@ -408,9 +408,11 @@ namespace vg
         const bool learned = !ext && m.scores != nullptr;
         const bool grouped = !ext && (learned || m.schedule >= 1);
         const bool wide = grouped && !learned && m.schedule == 2;
+        const bool packed = grouped && !learned && m.schedule == 3;
         const void *fn = ext ? r->edges_ext_fn[which]
-                                : learned ? r->edges_learned_fn[which]
-                                          : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
+                             : learned ? r->edges_learned_fn[which]
+                             : packed  ? r->edges_packed_fn[which]
+                                       : (wide ? r->edges_wide_fn[which] : (grouped ? r->edges_grouped_fn[which] : r->edges_fn[which]));
         int occ = 0;
         if (int rc = prepare_kernel(fn, smem, kBlock, &occ))
             return rc;
@@ -425,8 +427,9 @@ namespace vg
         EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes,
                       m.dist};
         const auto launch = ext ? r->edges_ext[which]
-                                   : learned ? r->edges_learned[which]
-                                             : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
+                                : learned ? r->edges_learned[which]
+                                : packed  ? r->edges_packed[which]
+                                          : (wide ? r->edges_wide[which] : (grouped ? r->edges_grouped[which] : r->edges[which]));
         VG_CUDA(launch(p, grid, kBlock, smem, s), "edges kernel launch");
         return VG_OK;
     }
@@ -707,8 +710,8 @@ int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode)
 
 int vg_env_set_schedule(vg_env *env, int schedule)
 {
-    if (!env || schedule < 0 || schedule > 2)
-        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0, 1 or 2");
+    if (!env || schedule < 0 || schedule > 3)
+        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0, 1, 2 or 3");
     env->schedule = schedule;
     env->tuned.clear();
     return VG_OK;

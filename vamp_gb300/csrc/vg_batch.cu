@@ -236,10 +236,13 @@ int vg_autotune_motions(const char *robot, vg_env *env, const float *a, const fl
     float best = 1e30f;
     const int which = env->lanes == 8 ? 0 : 1;
     const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
-    for (int sched = 0; sched < 3 && rc == VG_OK; ++sched)
+    for (int sched = 0; sched < 4 && rc == VG_OK; ++sched)
     {
         int occ = 0;
-        const void *fn = sched == 0 ? r->edges_fn[which] : (sched == 1 ? r->edges_grouped_fn[which] : r->edges_wide_fn[which]);
+        const void *fn = sched == 0   ? r->edges_fn[which]
+                         : sched == 1 ? r->edges_grouped_fn[which]
+                         : sched == 2 ? r->edges_wide_fn[which]
+                                      : r->edges_packed_fn[which];
         rc = prepare_kernel(fn, smem, kBlock, &occ);
         for (int bps = occ; bps >= 1 && rc == VG_OK; --bps)
         {

@@ -32,6 +32,10 @@ namespace vg
         // same-edge schedule compiled for fewer resident blocks (more registers per thread)
         cudaError_t (*edges_wide[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_wide_fn[2];
+        // the register-rich same-edge schedule with the segments an edge leaves free given to the
+        // next edge
+        cudaError_t (*edges_packed[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *edges_packed_fn[2];
         // same-edge schedule in a learned block order (EdgesParams::scores)
         cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_learned_fn[2];
@@ -80,7 +84,8 @@ namespace vg
     struct RobotTune
     {
         const RobotOps *robot;
-        int schedule;       // 0: a segment per edge, 1: a warp per edge, 2: a warp per edge, register-rich build
+        int schedule;       // 0: a segment per edge, 1: a warp per edge, 2: a warp per edge, register-rich build,
+                            // 3: as 2 with free segments starting on the next edge
         int blocks_per_sm;  // resident blocks per SM (0: as many as fit)
     };
 }  // namespace vg
@@ -147,7 +152,7 @@ namespace vg
         uint8_t *out;
         int32_t *blocks;
         unsigned *counter;     // work counter, cleared on the stream before the launch
-        int schedule = 1;      // 0: a segment per edge, 1: a warp per edge, 2: the same, register-rich build
+        int schedule = 1;      // 0: a segment per edge, 1: a warp per edge, 2: the same, register-rich build, 3: 2 packed
         int blocks_per_sm = 0;  // 0: as many as fit
         const float *dist = nullptr;  // validate_vector form: b holds vectors, dist their lengths
     };

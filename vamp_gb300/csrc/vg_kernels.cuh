@@ -593,6 +593,198 @@ namespace vg
         }
     }
 
+    // Packed same-edge schedule: as edges_grouped_kernel, except that the segments an edge's last
+    // blocks leave free start on the next edge instead of idling.  A warp iteration covers at
+    // most two edges: the one carried over from the previous iteration (its next blocks, from
+    // segment 0 on) and one taken from the queue (its first blocks, in the segments after those).
+    // Only the edge in the last segment can be carried over, so the carried edge's newest block
+    // always sits in the last segment: each segment takes that block's configuration and bs from
+    // the last segment (same lane of the segment) and subtracts bs seg + 1 more times.  Every
+    // block is therefore still block 0 minus bs repeated i times, as the reference computes it
+    // (planning/validate.hh:50-56), and verdicts and block counts equal edges_grouped_kernel's.
+    template <typename Robot, int W, int kMinBlocks = VG_MIN_BLOCKS, bool kLoopedEnv = VG_DEFAULT_LOOPED_ENV != 0>
+    __global__ void __launch_bounds__(128, kMinBlocks) edges_packed_kernel(EdgesParams p)
+    {
+        static_assert(W == 8 || W == 4, "packed schedule: 4 or 8 segments per warp");
+        extern __shared__ float4 smem[];
+        const EnvView ev = stage_env(p.env, smem);
+        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
+        constexpr int D = Robot::kDim;
+        constexpr int S = 32 / W;  // segments (blocks) per warp
+        const int lane = threadIdx.x & 31;
+        const int seg = lane / W;
+        const int sl = lane % W;
+        const int last = (S - 1) * W + sl;  // this lane's counterpart in the last segment
+        const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
+
+        float q[D], bs[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            q[d] = 0.0f;
+            bs[d] = 0.0f;
+        }
+        // warp-uniform: the carried edge (-1: none), its block count and its next block
+        int ce = -1, cn = 0, cpos = 0;
+        bool drained = false;  // warp-uniform: the queue is empty
+        for (;;)
+        {
+            // segments 0 .. r-1 continue the carried edge
+            const int r = ce >= 0 ? min(cn - cpos, S) : 0;
+            if (r > 0)
+            {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                {
+                    const float qs = __shfl_sync(kFull, q[d], last);
+                    const float bss = __shfl_sync(kFull, bs[d], last);
+                    if (seg < r)
+                    {
+                        q[d] = qs;
+                        bs[d] = bss;
+                    }
+                }
+                if (seg < r)
+                {
+#pragma unroll 1
+                    for (int k = 0; k <= seg; ++k)
+                    {
+#pragma unroll
+                        for (int d = 0; d < D; ++d)
+                        {
+                            q[d] = __fsub_rn(q[d], bs[d]);
+                        }
+                    }
+                }
+            }
+            // the remaining segments start on a new edge
+            int ne = -1, nn = 0;
+            if (r < S && !drained)
+            {
+                unsigned got = 0;
+                if (lane == 0)
+                {
+                    got = atomicAdd(p.head, 1u);
+                }
+                got = __shfl_sync(kFull, got, 0);
+                if (got >= static_cast<unsigned>(p.n))
+                {
+                    drained = true;
+                }
+                else
+                {
+                    ne = static_cast<int>(got);
+                }
+            }
+            if (ne >= 0)
+            {
+                float av[D], v[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                {
+                    av[d] = p.a[static_cast<long long>(ne) * D + d];
+                    v[d] = p.dist ? p.b[static_cast<long long>(ne) * D + d]
+                                  : __fsub_rn(p.b[static_cast<long long>(ne) * D + d], av[d]);
+                }
+                const float len = p.dist ? p.dist[ne] : edge_length<D>(v);
+                const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
+                const float nf = ceilf(t);
+                nn = static_cast<int>(nf > 1.0f ? nf : 1.0f);
+                if (seg >= r)
+                {
+                    const float denom = static_cast<float>(W * nn);
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                    {
+                        q[d] = __fmaf_rn(v[d], pct, av[d]);
+                        bs[d] = __fdiv_rn(v[d], denom);
+                    }
+#pragma unroll 1
+                    for (int k = r; k < seg; ++k)
+                    {
+#pragma unroll
+                        for (int d = 0; d < D; ++d)
+                        {
+                            q[d] = __fsub_rn(q[d], bs[d]);
+                        }
+                    }
+                }
+            }
+            const bool active = seg < r || (ne >= 0 && seg >= r && seg - r < nn);
+            const unsigned mask = __ballot_sync(kFull, active);
+            if (!mask)
+            {
+                break;  // nothing carried and the queue is empty
+            }
+            const unsigned alive = run_fkcc<Robot, W, kLoopedEnv>(ev, q, mask, stage);
+            const unsigned dead = mask & ~alive;
+            const unsigned cmask = r >= S ? kFull : ((1u << (r * W)) - 1u);  // the carried edge's lanes
+            if (ce >= 0)
+            {
+                const unsigned cd = dead & cmask;
+                int verdict = -1, checked = 0;
+                if (cd)
+                {
+                    verdict = 0;
+                    checked = cpos + (__ffs(cd) - 1) / W + 1;
+                }
+                else if (cpos + r >= cn)
+                {
+                    verdict = 1;
+                    checked = cn;
+                }
+                if (verdict >= 0)
+                {
+                    if (lane == 0)
+                    {
+                        p.out[ce] = static_cast<uint8_t>(verdict);
+                        if (p.blocks)
+                        {
+                            p.blocks[ce] = checked;
+                        }
+                    }
+                    ce = -1;
+                }
+                else
+                {
+                    cpos += r;  // r == S: no new edge this iteration
+                }
+            }
+            if (ne >= 0)
+            {
+                const unsigned nd = dead & ~cmask;
+                int verdict = -1, checked = 0;
+                if (nd)
+                {
+                    verdict = 0;
+                    checked = (__ffs(nd) - 1) / W - r + 1;
+                }
+                else if (nn <= S - r)
+                {
+                    verdict = 1;
+                    checked = nn;
+                }
+                if (verdict >= 0)
+                {
+                    if (lane == 0)
+                    {
+                        p.out[ne] = static_cast<uint8_t>(verdict);
+                        if (p.blocks)
+                        {
+                            p.blocks[ne] = checked;
+                        }
+                    }
+                }
+                else
+                {
+                    ce = ne;  // its blocks 0 .. S - r - 1 are checked, the last in the last segment
+                    cn = nn;
+                    cpos = S - r;
+                }
+            }
+        }
+    }
+
     // The same-edge schedule with the four warps of a block kept in step: one barrier per check
     // iteration, so that the block's warps run the same part of the check at about the same time
     // and share its instruction-cache lines.  Same blocks, same order, same verdicts and block

@@ -38,6 +38,13 @@ namespace vg
         return cudaGetLastError();
     }
 
+    template <typename R, int W, int kMinBlocks, bool kLoopedEnv>
+    cudaError_t launch_edges_packed(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        edges_packed_kernel<R, W, kMinBlocks, kLoopedEnv><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
     template <typename R, int W>
     cudaError_t launch_edges_lockstep(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
@@ -103,6 +110,10 @@ namespace vg
         o.edges_wide[1] = &launch_edges_grouped<R, 4, false, VG_MIN_BLOCKS_WIDE, true>;
         o.edges_wide_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false, VG_MIN_BLOCKS_WIDE, true>);
         o.edges_wide_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false, VG_MIN_BLOCKS_WIDE, true>);
+        o.edges_packed[0] = &launch_edges_packed<R, 8, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_packed[1] = &launch_edges_packed<R, 4, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_packed_fn[0] = reinterpret_cast<const void *>(&edges_packed_kernel<R, 8, VG_MIN_BLOCKS_WIDE, true>);
+        o.edges_packed_fn[1] = reinterpret_cast<const void *>(&edges_packed_kernel<R, 4, VG_MIN_BLOCKS_WIDE, true>);
         o.edges_learned[0] = &launch_edges_grouped<R, 8, true>;
         o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
         o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);
