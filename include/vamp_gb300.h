@@ -138,9 +138,11 @@ int vg_eefk(const char *robot, const float *q, size_t n, float *out);
 /* Which reference build to reproduce: lanes 8 + VG_SQRT_X86 (default) or lanes 4 + VG_SQRT_EXACT. */
 int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode);
 /* How vg_validate_motions schedules edges on the GPU (verdicts are the same either way):
- * 1 (default) = a warp checks consecutive blocks of one edge, 0 = each lane-block checks its own
- * edge, 2 = as 1 with the kernel built for fewer resident blocks and more registers per thread,
- * 3 = as 2 with the segments an edge's last blocks leave free starting on the next edge.
+ * 1 = a warp checks consecutive blocks of one edge, 0 = each lane-block checks its own edge, 2 = as
+ * 1 with the kernel built for fewer resident blocks and more registers per thread, 3 = as 2 with
+ * the segments an edge's last blocks leave free starting on the next edge, -1 (default) = each
+ * robot's own (2 for the Panda, UR5 and Fetch, 1 for Baxter).  An autotuner pick
+ * (vg_autotune_motions) takes precedence until this is called again.
  * No reference counterpart: the reference validates one edge at a time on one core. */
 int vg_env_set_schedule(vg_env *env, int schedule);
 /* Number of objects of a kind (0 spheres, 1 capsules, 2 z-capsules, 3 cuboids, 4 z-cuboids)

@@ -190,7 +190,7 @@ def test_both_edge_schedules_agree_with_the_oracle(vg, port, torch, lanes, sqrt_
     a, b = scenes.edges(rb.s_m, rb.s_a, 8192, 88)
     cpu, cpu_blocks = port.env(scene, sqrt_mode=SQRT_X86 if sqrt_mode == 0 else SQRT_EXACT).validate_motions(
         rb, a, b, 32, lanes=lanes, threads=THREADS)
-    for schedule in (0, 1, 2, 3):
+    for schedule in (-1, 0, 1, 2, 3):
         env = vg.Environment.from_scene(scene, lanes=lanes, sqrt_mode=sqrt_mode)
         env.set_schedule(schedule)
         blocks = torch.zeros(len(a), dtype=torch.int32, device="cuda")

@@ -68,9 +68,10 @@ class Environment:
         self.lanes, self.sqrt_mode = lanes, sqrt_mode
 
     def set_schedule(self, schedule: int) -> None:
-        """GPU edge schedule: 1 (default) a warp per edge, 0 a lane-block per edge, 2 a warp per
-        edge with the register-rich build, 3 as 2 with the segments an edge leaves free starting
-        on the next edge.  Verdicts and block counts are the same in every schedule."""
+        """GPU edge schedule: 1 a warp per edge, 0 a lane-block per edge, 2 a warp per edge with
+        the register-rich build, 3 as 2 with the segments an edge leaves free starting on the
+        next edge, -1 (default) each robot's own (2 for the Panda, UR5 and Fetch, 1 for Baxter).
+        Verdicts and block counts are the same in every schedule."""
         check(lib.vg_env_set_schedule(self._h, schedule))
 
     def add_sphere(self, sphere) -> None:

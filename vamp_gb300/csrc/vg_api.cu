@@ -383,7 +383,7 @@ namespace vg
 
     void tuned_for(const vg_env *env, const RobotOps *r, int *schedule, int *blocks_per_sm)
     {
-        *schedule = env->schedule;
+        *schedule = env->schedule >= 0 ? env->schedule : r->default_schedule;
         *blocks_per_sm = 0;
         for (const RobotTune &t : env->tuned)
         {
@@ -710,8 +710,8 @@ int vg_env_set_mode(vg_env *env, int lanes, int sqrt_mode)
 
 int vg_env_set_schedule(vg_env *env, int schedule)
 {
-    if (!env || schedule < 0 || schedule > 3)
-        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be 0, 1, 2 or 3");
+    if (!env || schedule < -1 || schedule > 3)
+        return set_error(VG_ERR_ARG, "vg_env_set_schedule: schedule must be -1, 0, 1, 2 or 3");
     env->schedule = schedule;
     env->tuned.clear();
     return VG_OK;

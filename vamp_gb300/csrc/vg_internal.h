@@ -18,6 +18,7 @@ namespace vg
     {
         const char *name;
         int dim, fine, slots, resolution;
+        int default_schedule;  // edge schedule when the environment has neither a pick nor a setting
         float r_min, r_max;
         const float *s_m;
         const float *s_a;
@@ -99,7 +100,8 @@ struct vg_env
     int n_added = 0;
     int lanes = 8;
     int sqrt_mode = 0;
-    int schedule = 1;  // 0: a segment per edge, 1: a warp per edge (consecutive blocks)
+    int schedule = -1;  // -1: each robot's default; 0: a segment per edge, 1: a warp per edge (consecutive
+                        // blocks), 2: 1 register-rich, 3: 2 packed
     bool dirty = true;
     int device = -1;
     // device image

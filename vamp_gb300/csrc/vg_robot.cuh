@@ -77,10 +77,11 @@ namespace vg
     }
 
     template <typename R>
-    RobotOps make_robot_ops()
+    RobotOps make_robot_ops(int default_schedule)
     {
         RobotOps o{};
         o.name = R::kName;
+        o.default_schedule = default_schedule;
         o.dim = R::kDim;
         o.fine = R::kFine;
         o.slots = R::kSlots;
@@ -134,9 +135,11 @@ namespace vg
     }
 }  // namespace vg
 
-#define VG_DEFINE_ROBOT(Type, var)                                                 \
+// `schedule`: the edge schedule of an environment that was neither autotuned for the robot nor
+// given one (vg_env_set_schedule); the autotuner's pick for the robot on its own edge workloads.
+#define VG_DEFINE_ROBOT(Type, var, schedule)                                       \
     namespace vg                                                                   \
     {                                                                              \
         extern const RobotOps var;                                                 \
-        const RobotOps var = make_robot_ops<vg::robots::Type>();                   \
+        const RobotOps var = make_robot_ops<vg::robots::Type>(schedule);           \
     }
