@@ -122,8 +122,13 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "10"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a while to start: wait (2 s at most) for its first row so that
+            # the timed region, often well under a second, falls between samples it takes
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 2.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
