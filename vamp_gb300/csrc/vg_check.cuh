@@ -696,8 +696,10 @@ namespace vg
     constexpr int kWarpScratch = 64;
 
     // The context a generated Robot::fkcc body runs against.  kExt: the environment queries also
-    // test heightfields.
-    template <int W, bool kExtended = false>
+    // test heightfields.  kOrdered: the warp's segments are consecutive blocks of one edge in the
+    // reference's order (the same-edge schedule), so only the first colliding segment decides the
+    // edge's verdict and block count.
+    template <int W, bool kExtended = false, bool kOrdered = false>
     struct CheckCtx
     {
         static constexpr int kW = W;
@@ -735,6 +737,22 @@ namespace vg
             return self_query<W>(ax, ay, az, ar, bx, by, bz, br, mask);
         }
 
+        // Removes the colliding segments `hit` from alive and returns what is left.  kOrdered:
+        // the segments after the first colliding one go too, since no result of theirs can
+        // change the verdict or the block count (the first colliding block stays the first).
+        __device__ __forceinline__ unsigned kill(unsigned hit)
+        {
+            if constexpr (kOrdered)
+            {
+                alive &= hit ? (1u << (__ffs(hit) - 1)) - 1u : kFull;
+            }
+            else
+            {
+                alive &= ~hit;
+            }
+            return alive;
+        }
+
         // the segments in `mask` for which any OR-accumulated sign bit is set
         __device__ __forceinline__ unsigned vote(unsigned bits, unsigned mask)
         {
@@ -755,11 +773,11 @@ namespace vg
             if (hit)
             {
                 need &= ~hit;
-                ctx.alive &= ~hit;
-                if (!ctx.alive)
+                if (!ctx.kill(hit))
                 {
                     return true;
                 }
+                need &= ctx.alive;
                 if (!need)
                 {
                     return false;
@@ -787,11 +805,11 @@ namespace vg
                 if (hit)
                 {
                     need &= ~hit;
-                    ctx.alive &= ~hit;
-                    if (!ctx.alive)
+                    if (!ctx.kill(hit))
                     {
                         return true;
                     }
+                    need &= ctx.alive;
                     if (!need)
                     {
                         return false;

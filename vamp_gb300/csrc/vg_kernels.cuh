@@ -161,13 +161,14 @@ namespace vg
     // kExt: the extended checks, for environments with heightfields or an attachment: every
     // environment query also tests the heightfields, and with an attachment the block runs
     // Robot::fkcc_attach
-    template <typename Robot, int W, bool kLoopedEnv = false, bool kExt = false>
+    // kOrdered: the segments are consecutive blocks of one edge (CheckCtx)
+    template <typename Robot, int W, bool kLoopedEnv = false, bool kExt = false, bool kOrdered = false>
     __device__ __forceinline__ unsigned run_fkcc(const EnvView &ev, const float *q, unsigned alive, float *stage)
     {
         static_assert(Robot::kEnvChecks <= kWarpScratch, "per-warp scratch holds one word per environment check");
         __shared__ unsigned warp_scratch[kStageStride / 32][kWarpScratch];
-        CheckCtx<W, kExt> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
-        Robot::template fkcc<CheckCtx<W, kExt>, kLoopedEnv>(q, ctx);
+        CheckCtx<W, kExt, kOrdered> ctx{ev, alive, false, stage, warp_scratch[threadIdx.x >> 5]};
+        Robot::template fkcc<CheckCtx<W, kExt, kOrdered>, kLoopedEnv>(q, ctx);
         if constexpr (kExt)
         {
             if (ctx.alive && ev.n_att >= 0)
@@ -533,7 +534,7 @@ namespace vg
                         }
                     }
                     const unsigned mask = __ballot_sync(kFull, active);
-                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv>(ev, q, mask, stage);
+                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv, false, true>(ev, q, mask, stage);
                     const unsigned dead = mask & ~alive;
                     // one bit per active segment (its first lane)
                     const unsigned leaders = mask & kSegLeaders;
@@ -562,7 +563,7 @@ namespace vg
                 {
                     const bool active = i0 + seg < n;
                     const unsigned mask = __ballot_sync(kFull, active);
-                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv>(ev, q, mask, stage);
+                    const unsigned alive = run_fkcc<Robot, W, kLoopedEnv, false, true>(ev, q, mask, stage);
                     const unsigned dead = mask & ~alive;
                     if (dead)
                     {

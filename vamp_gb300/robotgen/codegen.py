@@ -813,7 +813,7 @@ def gen_cuda(model: dict) -> str:
                 const float4 s = centre(F, {pre}EnvFine[i]);
                 const unsigned hit = ctx.env_hit(s.x, s.y, s.z, s.w, need);
                 need &= ~hit;
-                if (hit && !(ctx.alive &= ~hit))
+                if (hit && !ctx.kill(hit))
                 {{
                     return;
                 }}
@@ -857,7 +857,7 @@ def gen_cuda(model: dict) -> str:
                 }}
             }}
             const unsigned hit = ctx.vote(acc, need);
-            if (hit && !(ctx.alive &= ~hit))
+            if (hit && !ctx.kill(hit))
             {{
                 return;
             }}
@@ -930,7 +930,7 @@ def gen_cuda(model: dict) -> str:
                 out.append(f"        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, st, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
             else:
                 out.append(f"        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, {fa}, {env_start[k]}, {env_start[k + 1]}, need);")
-            out.append("        if (hit && !(ctx.alive &= ~hit)) return;")
+            out.append("        if (hit && !ctx.kill(hit)) return;")
             out.append("    }")
             out.append("}")
         return out
@@ -965,7 +965,7 @@ def gen_cuda(model: dict) -> str:
                 out.append(f"        const unsigned acc = ctx.in_limits ? self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}LivePair, {lv_start[ci]}, {lv_start[ci + 1]})")
                 out.append(f"                                           : self_pairs({frame_expr(fa)}, {frame_expr(fb)}, {pre}FullPair, {full_start[ci]}, {full_start[ci + 1]});")
             out.append("        const unsigned hit = ctx.vote(acc, need);")
-            out.append("        if (hit && !(ctx.alive &= ~hit)) return;")
+            out.append("        if (hit && !ctx.kill(hit)) return;")
             out.append("    }")
             out.append("}")
         return out
@@ -1006,7 +1006,7 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
             acc = self_pairs(st, t.z, t.w, {pre}FullPair, u.z, u.w, cbc);
         }}
         const unsigned hit = ctx.vote(acc, need);
-        if (hit && !(ctx.alive &= ~hit)) return;
+        if (hit && !ctx.kill(hit)) return;
     }}
 }}""".split("\n")
     staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
@@ -1047,7 +1047,7 @@ for (int k = 0; k < {n_env}; ++k)
     if (need)
     {{
         const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
-        if (hit && !(ctx.alive &= ~hit)) return;
+        if (hit && !ctx.kill(hit)) return;
     }}
 }}""".split("\n")
     # the environment section either as loops (one copy of the batched query: small code) or
