@@ -33,7 +33,10 @@ sys.path.insert(0, str(ROOT))
 N_EDGES = 65536
 RESOLUTION = 32
 SCENE_SEED = 1
-EDGE_SEED = 2024
+EDGE_SEED = 2024  # the mixed workload's edges (one seed per robot from here)
+# The first correct version of the plain GPU path (a segment per edge, per-object votes) checked
+# this workload in 9.58 ms: the learned-order target is stated against it.
+FIRST_VERSION_EDGES_PER_S = N_EDGES / 9.58e-3
 METRIC = "edges validated/s on 1 GB300, learned-order vs plain GPU path, identical verdicts"
 WORKLOAD = "panda validate_motion batch: 65536 edges, res 32, 24 spheres + 24 cuboids + 12 capsules"
 
@@ -99,9 +102,31 @@ def workload():
     m = model("panda")
     s_m = np.array(m["s_m"], np.float32)
     s_a = np.array(m["s_a"], np.float32)
-    scene = scenes.scene_config1(SCENE_SEED)
-    a, b = scenes.edges(s_m, s_a, N_EDGES, EDGE_SEED)
-    return scene, a, b
+    return scenes.workload_config1(s_m, s_a)
+
+
+def reference_flips(scene, a, b, verdicts: dict, blocks: dict) -> dict:
+    """Differences from the compiled reference's own verdicts and block counts on this workload
+    (tests/golden/full_config1.npz, written by tests/golden/make_golden.py).  verdicts / blocks:
+    per path, as numpy arrays (blocks None where a path checks blocks in another order).  A flip
+    is explained only for a state within 1e-5 m of contact; the classification needs the CPU
+    oracle and runs in tests/test_full_configs.py, so a nonzero count here is reported as
+    unclassified (null)."""
+    from vamp_gb300 import scenes
+
+    with np.load(ROOT / "tests" / "golden" / "full_config1.npz") as f:
+        g = {k: f[k] for k in f.files}
+    inputs = [scene.get(k, np.zeros((0, 1), np.float32)) for k in ("spheres", "capsules", "cuboids")]
+    if scenes.input_digest(*inputs, a, b) != str(g["digest"]):
+        return {"available": False, "why": "the workload's inputs differ from those of the fixture"}
+    ref = np.unpackbits(g["verdict"])[: int(g["n"])]
+    out = {"available": True, "reference": "compiled reference, x86-64 AVX2 build (8 lanes)"}
+    for path, v in verdicts.items():
+        n = int((v != ref).sum())
+        out[path] = {"vs_reference": n, "unexplained": 0 if n == 0 else None}
+        if blocks.get(path) is not None:
+            out[path]["block_counts_differ"] = int((blocks[path] != g["blocks"]).sum())
+    return out
 
 
 class ClockSampler:
@@ -275,10 +300,10 @@ def run_capt(args, world, rank, local):
     dev = torch.device("cuda", local)
     m = model("panda")
     s_m, s_a = np.array(m["s_m"], np.float32), np.array(m["s_a"], np.float32)
-    pts = scenes.surface_pointcloud(SCENE_SEED, 50_000)
+    scene, q_np, a_np, b_np = scenes.workload_config2(s_m, s_a, m["min_radius"], m["max_radius"])
+    pts = scene["pointclouds"][0]["points"]
     t0 = time.perf_counter()
-    env = vg.Environment.from_scene({"pointclouds": [{"points": pts, "r_min": m["min_radius"], "r_max": m["max_radius"],
-                                                       "r_point": scenes.POINT_RADIUS}]})
+    env = vg.Environment.from_scene(scene)
     build_s = time.perf_counter() - t0
     # the same tree built on the GPU (vg_env_add_pointcloud_device; synchronous), first call untimed
     pts_dev = torch.from_numpy(pts).to(dev)
@@ -288,8 +313,7 @@ def run_capt(args, world, rank, local):
         vg.Environment().add_pointcloud_device(pts_dev, m["min_radius"], m["max_radius"], scenes.POINT_RADIUS)
         if i:
             gpu_build.append(time.perf_counter() - t0)
-    q = torch.from_numpy(scenes.configurations(s_m, s_a, 1 << 20, 77)).to(dev)
-    a_np, b_np = scenes.edges(s_m, s_a, 16384, 78)
+    q = torch.from_numpy(q_np).to(dev)
     a, b = torch.from_numpy(a_np).to(dev), torch.from_numpy(b_np).to(dev)
     qo = torch.empty(len(q), dtype=torch.uint8, device=dev)
     eo = torch.empty(len(a), dtype=torch.uint8, device=dev)
@@ -318,9 +342,17 @@ def run_capt(args, world, rank, local):
             torch.cuda.synchronize()
             ts.append(s0.elapsed_time(s1))
         res[name] = float(np.mean(ts))
+    with np.load(ROOT / "tests" / "golden" / "full_config2.npz") as f:
+        g = {k: f[k] for k in f.files}
+    if scenes.input_digest(pts, q_np, a_np, b_np) == str(g["digest"]):
+        flips = {"states_vs_reference": int((qo.cpu().numpy() != np.unpackbits(g["state_verdict"])[: len(q_np)]).sum()),
+                 "edges_vs_reference": int((eo.cpu().numpy() != np.unpackbits(g["edge_verdict"])[: len(a_np)]).sum()),
+                 "reference": "compiled reference, x86-64 AVX2 build (8 lanes), tests/golden/full_config2.npz"}
+    else:
+        flips = {"available": False, "why": "the workload's inputs differ from those of the fixture"}
     if rank == 0:
         print(json.dumps({
-            "metric": "pointcloud (CAPT) checks on 1 GB300", "workload": "panda + 50k surface points",
+            "metric": "pointcloud (CAPT) checks on 1 GB300", "workload": "panda + 50k surface points", "flips": flips,
             "states_per_s": (1 << 20) / (res["states"] / 1e3), "states_ms": res["states"],
             "edges_per_s": 16384 / (res["edges"] / 1e3), "edges_ms": res["edges"],
             "capt_build_s": build_s, "capt_build_gpu_s": float(np.median(gpu_build)), "capt_blocks": int(env.pointcloud_layout(0)["aff_starts"][-1]),
@@ -673,6 +705,7 @@ def measure_learned(args, env, a, b, plain_out, stream, flush, dev, probes: int 
     lib.vg_mlp_destroy(m)
     rows = N_EDGES * probes
     return {
+        "_verdicts": lv,
         "verdicts_identical": bool(np.array_equal(pv, lv)),
         "edges_per_s": N_EDGES / ((score_ms + check_ms) / 1e3),
         "ms_per_step": score_ms + check_ms,
@@ -732,6 +765,9 @@ def run_gpu(args, world, rank, local):
     kernel_ms = float(np.mean(step_ms))
     kernel_ms = max_over_ranks(world, kernel_ms)
     value = world * N_EDGES / (kernel_ms / 1e3)
+    plain_blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)  # untimed: the block counts
+    check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
+                                         out.data_ptr(), plain_blocks.data_ptr(), stream.cuda_stream))
     learned = None if args.no_learned else measure_learned(args, env, a, b, out, stream, flush, dev)
 
     # end to end through the C ABI with host buffers
@@ -787,8 +823,16 @@ def run_gpu(args, world, rank, local):
                                 f"algorithmic FLOPs counted by the CPU oracle on 8192 of the edges, scaled"}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, a_np, b_np)
+    line["vs_first_version"] = value / FIRST_VERSION_EDGES_PER_S
+    paths = {"plain": gpu_verdicts}
+    path_blocks = {"plain": plain_blocks.cpu().numpy()}
     if learned is not None:
+        paths["learned"] = learned.pop("_verdicts")
+        path_blocks["learned"] = None
+        learned["learned_over_plain"] = learned["edges_per_s"] / value
+        learned["vs_first_version"] = learned["edges_per_s"] / FIRST_VERSION_EDGES_PER_S
         line["learned"] = learned
+    line["flips"] = reference_flips(scene, a_np, b_np, paths, path_blocks)
     print(json.dumps(line))
 
 

@@ -75,6 +75,35 @@ namespace
     thread_local std::size_t Recorder::count = 0;
     thread_local long Recorder::fail_at = -1;
 
+    // A stand-in robot whose fkcc forwards every block to the real Robot::fkcc and counts it:
+    // driving the reference's own validate_motion with it gives the verdict together with the
+    // number of blocks the reference checked before it stopped (planning/validate.hh:24-67).
+    // Environments with an attachment are not supported (the reference's fkcc_attach poses the
+    // attachment with Eigen, which the type-only stand-in cannot evaluate).
+    struct Counted
+    {
+        static constexpr std::size_t dimension = Robot::dimension;
+        using Configuration = Robot::Configuration;
+        template <std::size_t rake>
+        using ConfigurationBlock = Robot::ConfigurationBlock<rake>;
+
+        static thread_local std::size_t count;
+
+        template <std::size_t rake>
+        static bool fkcc(const collision::Environment<FloatVector<rake>> &e, const ConfigurationBlock<rake> &b) noexcept
+        {
+            ++count;
+            return Robot::template fkcc<rake>(e, b);
+        }
+
+        template <std::size_t rake>
+        static bool fkcc_attach(const collision::Environment<FloatVector<rake>> &e, const ConfigurationBlock<rake> &b) noexcept
+        {
+            return fkcc<rake>(e, b);
+        }
+    };
+    thread_local std::size_t Counted::count = 0;
+
     inline auto to_config(const float *q) -> Robot::Configuration
     {
         Robot::ConfigurationArray a;
@@ -281,6 +310,32 @@ void VG_FN(_validate_motions)(
         [&](std::size_t i)
         {
             out[i] = motion<Robot>(a + i * Robot::dimension, b + i * Robot::dimension, resolution, ev) ? 1 : 0;
+        });
+}
+
+// As _validate_motions, with the number of blocks the reference checked per edge (its early
+// return on the first colliding block included) in blocks[n].
+void VG_FN(_validate_motions_counted)(
+    void *env,
+    const float *a,
+    const float *b,
+    std::size_t n,
+    int resolution,
+    uint8_t *out,
+    int32_t *blocks,
+    int nthreads)
+{
+    auto *e = static_cast<RefEnv *>(env);
+    e->finalize();
+    const auto &ev = *e->vec;
+    parallel_for(
+        n,
+        nthreads,
+        [&](std::size_t i)
+        {
+            Counted::count = 0;
+            out[i] = motion<Counted>(a + i * Robot::dimension, b + i * Robot::dimension, resolution, ev) ? 1 : 0;
+            blocks[i] = static_cast<int32_t>(Counted::count);
         });
 }
 

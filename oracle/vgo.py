@@ -33,10 +33,21 @@ def build_port(force: bool = False) -> Path:
     return PORT_LIB
 
 
+def reference_checkout(reference: str | None = None) -> Path | None:
+    """The reference checkout named by the argument or, failing that, by VG_REFERENCE (None if
+    neither names a directory holding the reference's sources)."""
+    name = reference or os.environ.get("VG_REFERENCE")
+    if not name:
+        return None
+    ref = Path(name)
+    return ref if (ref / "src" / "impl" / "vamp").is_dir() else None
+
+
 def build_reference(reference: str | None = None) -> Path | None:
-    """Compile the reference oracle from the reference checkout, if present and on x86-64."""
-    ref = Path(reference or os.environ.get("VG_REFERENCE", "/root/reference"))
-    if not (ref / "src" / "impl" / "vamp").is_dir() or os.uname().machine != "x86_64":
+    """Compile the reference oracle from the reference checkout (argument or VG_REFERENCE), if
+    there is one and the host is x86-64."""
+    ref = reference_checkout(reference)
+    if ref is None or os.uname().machine != "x86_64":
         return None
     subprocess.run(
         ["make", "-s", "-j4", "-C", str(HERE / "ref"), f"REF_SRC={ref / 'src' / 'impl'}"], check=True
@@ -391,6 +402,8 @@ class Reference:
             getattr(lib, f"vgref_{r}_fkcc_block").argtypes = [_p, _p]
             getattr(lib, f"vgref_{r}_validate_states").argtypes = [_p, _p, _sz, _p, ctypes.c_int]
             getattr(lib, f"vgref_{r}_validate_motions").argtypes = [_p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
+            getattr(lib, f"vgref_{r}_validate_motions_counted").argtypes = [_p, _p, _p, _sz, ctypes.c_int, _p, _p,
+                                                                             ctypes.c_int]
             getattr(lib, f"vgref_{r}_filter_self").argtypes = [_p, _p, _sz, _f, _p, _p]
             getattr(lib, f"vgref_{r}_filter_self").restype = _sz
             getattr(lib, f"vgref_{r}_validate_vectors").argtypes = [_p, _p, _p, _p, _sz, ctypes.c_int, _p, ctypes.c_int]
@@ -537,6 +550,17 @@ class RefEnv:
             self.h, _ptr(a), _ptr(b), len(a), resolution, _ptr(out), threads
         )
         return out
+
+    def validate_motions_counted(self, robot: str, a, b, resolution: int, threads: int = 1):
+        """validate_motion per edge with the blocks the reference checked: (verdicts, blocks)."""
+        a = np.ascontiguousarray(a, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        out = np.zeros(len(a), np.uint8)
+        blocks = np.zeros(len(a), np.int32)
+        getattr(self.ref.lib, f"vgref_{robot}_validate_motions_counted")(
+            self.h, _ptr(a), _ptr(b), len(a), resolution, _ptr(out), _ptr(blocks), threads
+        )
+        return out, blocks
 
     def fkcc_block(self, robot: str, q_lanes_dim: np.ndarray) -> int:
         """q is [8][dim]; the reference takes [dim][8]."""

@@ -4,7 +4,7 @@ The reference (CoMMALab/vamp) ships no tests and no golden vectors, so the fixtu
 by running the reference itself: its hot-path headers compiled from the reference checkout by
 oracle/ref/Makefile (x86-64, AVX2 build, 8 lanes).  Run in a container that has the checkout:
 
-    python tests/golden/make_golden.py [--reference /path/to/vamp]
+    python tests/golden/make_golden.py --reference /path/to/vamp   (or VG_REFERENCE=/path/to/vamp)
 
 Every fixture stores its inputs as well as the reference's outputs, so the tests need neither the
 reference nor a particular random-number generator.
@@ -12,6 +12,7 @@ reference nor a particular random-number generator.
 from __future__ import annotations
 
 import argparse
+import os
 import sys
 from pathlib import Path
 
@@ -150,12 +151,49 @@ def filter_self_fixtures(ref: Reference) -> None:
     np.savez_compressed(OUT / "filter_self_panda.npz", **out)
 
 
+def scene_inputs(scene: dict) -> list:
+    """The arrays that define a scene, in a fixed order (for input_digest)."""
+    out = [scene.get(k, np.zeros((0, 1), np.float32)) for k in ("spheres", "capsules", "cuboids")]
+    out += [pc["points"] for pc in scene.get("pointclouds", [])]
+    return out
+
+
+def full_fixtures(ref: Reference) -> None:
+    """The reference's verdicts (and blocks checked per edge) on the benchmark configurations at
+    full size: config 0 (4,096 states), config 1 (65,536 edges at resolution 32) and config 2
+    (1,048,576 states and 16,384 edges against a 50,000-point cloud).  Only the inputs' digest is
+    stored; the tests regenerate the inputs from their seeds (vamp_gb300.scenes.workload_config*)."""
+    rb = Port().robot("panda")
+    threads = os.cpu_count() or 1
+    scene, q = scenes.workload_config0(rb.s_m, rb.s_a)
+    v = ref.env(scene).validate_states("panda", q, threads)
+    np.savez_compressed(OUT / "full_config0.npz", digest=scenes.input_digest(*scene_inputs(scene), q),
+                        verdict=np.packbits(v), n=len(q))
+    scene, a, b = scenes.workload_config1(rb.s_m, rb.s_a)
+    v, blocks = ref.env(scene).validate_motions_counted("panda", a, b, 32, threads)
+    np.savez_compressed(OUT / "full_config1.npz", digest=scenes.input_digest(*scene_inputs(scene), a, b),
+                        verdict=np.packbits(v), blocks=blocks.astype(np.uint16), n=len(a), resolution=32)
+    from vamp_gb300.robots import model
+
+    m = model("panda")
+    scene, q, a, b = scenes.workload_config2(rb.s_m, rb.s_a, m["min_radius"], m["max_radius"])
+    renv = ref.env(scene)
+    sv = renv.validate_states("panda", q, threads)
+    ev, blocks = renv.validate_motions_counted("panda", a, b, 32, threads)
+    np.savez_compressed(OUT / "full_config2.npz", digest=scenes.input_digest(*scene_inputs(scene), q, a, b),
+                        state_verdict=np.packbits(sv), n_states=len(q), edge_verdict=np.packbits(ev),
+                        blocks=blocks.astype(np.uint16), n_edges=len(a), resolution=32)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=None)
-    ap.add_argument("--only", choices=["filter", "eefk", "heightfield", "vectors", "filter_self"], default=None,
+    ap.add_argument("--reference", default=os.environ.get("VG_REFERENCE"),
+                    help="the reference checkout (default: $VG_REFERENCE)")
+    ap.add_argument("--only", choices=["filter", "eefk", "heightfield", "vectors", "filter_self", "full"], default=None,
                     help="regenerate one group of fixtures")
     a = ap.parse_args()
+    if not a.reference:
+        raise SystemExit("name the reference checkout with --reference or VG_REFERENCE")
     if build_reference(a.reference) is None:
         raise SystemExit("reference checkout not found (or not x86-64): cannot generate golden fixtures")
     ref = Reference()
@@ -163,13 +201,15 @@ def main():
     if a.only in (None, "filter"):
         filter_fixtures(ref)
     if a.only in (None, "eefk"):
-        eefk_fixtures(Path(a.reference or "/root/reference"))
+        eefk_fixtures(Path(a.reference))
     if a.only in (None, "heightfield"):
         heightfield_fixtures(ref)
     if a.only in (None, "vectors"):
         vector_fixtures(ref)
     if a.only in (None, "filter_self"):
         filter_self_fixtures(ref)
+    if a.only in (None, "full"):
+        full_fixtures(ref)
     if a.only is not None:
         return
 

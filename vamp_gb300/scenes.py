@@ -195,3 +195,41 @@ def scene_config0(seed: int = 0) -> dict:
 def scene_config1(seed: int = 1) -> dict:
     """Config 1: 24 spheres, 24 cuboids, 12 capsules placed in the 4 m workspace volume."""
     return primitive_scene(seed, 24, 24, 12, "workspace")
+
+
+# The seeded inputs of the benchmark configurations at full size (one definition, shared by the
+# benchmark, the tests and the fixture generator).
+
+def workload_config0(s_m, s_a):
+    """Config 0: the config-0 scene and 4,096 configurations uniform within the joint limits."""
+    return scene_config0(0), configurations(s_m, s_a, 4096, 4096)
+
+
+def workload_config1(s_m, s_a):
+    """Config 1: the config-1 scene (seed 1) and 65,536 edges with endpoints uniform within the
+    joint limits (seed 2024); checked at resolution 32."""
+    a, b = edges(s_m, s_a, 65536, 2024)
+    return scene_config1(1), a, b
+
+
+def workload_config2(s_m, s_a, r_min: float, r_max: float):
+    """Config 2: 50,000 points on the surfaces of 30 cuboids and capsules plus 2 % noise (seed 1),
+    whose tree is built with the robot's sphere radius range; 1,048,576 configurations (seed 77)
+    and 16,384 edges (seed 78) at resolution 32."""
+    pts = surface_pointcloud(1, 50_000)
+    scene = {"pointclouds": [{"points": pts, "r_min": r_min, "r_max": r_max, "r_point": POINT_RADIUS}]}
+    q = configurations(s_m, s_a, 1 << 20, 77)
+    a, b = edges(s_m, s_a, 16384, 78)
+    return scene, q, a, b
+
+
+def input_digest(*arrays) -> str:
+    """SHA-256 of the arrays' float32 bytes, in order: fixtures of the reference's verdicts on the
+    workloads above record it, so that a change of the seeded generator is caught instead of
+    comparing verdicts of different inputs."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for x in arrays:
+        h.update(np.ascontiguousarray(x, np.float32).tobytes())
+    return h.hexdigest()
