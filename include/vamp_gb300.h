@@ -69,6 +69,20 @@ int vg_env_add_capsule(vg_env *env, const float *fields8);
 /* Cuboid: centre xyz, axis_1 xyz, axis_2 xyz, axis_3 xyz, half extents (collision/shapes.hh:29-120);
  * stored as z-aligned when axis_3_z == 1 (bindings/environment.cc:118-131). */
 int vg_env_add_cuboid(vg_env *env, const float *fields15);
+/* One primitive in the kind list the caller chose (0 spheres, 1 capsules, 2 z-aligned capsules,
+ * 3 cuboids, 4 z-aligned cuboids; fields as vg_env_add_sphere / _capsule / _cuboid) with the
+ * min_distance the caller computed: the form a converted collision::Environment<FloatVector<rake>>
+ * needs (collision/environment.hh:15-85), whose objects already sit in their kind lists
+ * (Shape::min_distance, collision/shapes.hh:9-12).  Kept sorted by min_distance, as
+ * Environment::sort (collision/environment.hh:43-69) leaves them. */
+int vg_env_add_primitive(vg_env *env, int kind, const float *fields, float min_distance);
+/* A pointcloud tree as the reference built it (collision/capt.hh:584-617), in the layout
+ * vg_env_pointcloud_layout returns: tests[2^nlog2 - 1], aabbs[2^nlog2][6], aff_starts[2^nlog2 + 1]
+ * (non-decreasing, in 8-point blocks, the last equal to n_blocks), aff[n_blocks][3][8], top[6],
+ * and the tree's r_min, r_max, r_point.  For converting a collision::CAPT without rebuilding it. */
+int vg_env_add_pointcloud_layout(vg_env *env, int nlog2, const float *tests, const float *aabbs, const uint32_t *aff_starts,
+                                 const float *aff, size_t n_blocks, const float *top, float r_min, float r_max,
+                                 float r_point);
 /* A pointcloud, checked as a CAPT built exactly as the reference builds it
  * (collision/capt.hh:294-365; Environment.add_pointcloud, bindings/environment.cc:150-161):
  * xyz is [n][3], n >= 2; queries pad sphere radii by r_point; the tree affords points for radii
@@ -129,6 +143,9 @@ int vg_env_add_heightfield(vg_env *env, const float *centre, const float *scale,
  * the robot links the reference lists.  At most VG_MAX_ATTACH_SPHERES spheres. */
 #define VG_MAX_ATTACH_SPHERES 64
 int vg_env_attach(vg_env *env, const float *tf16, const float *spheres, size_t k);
+/* A heightfield from the fields a collision::HeightField stores (collision/shapes.hh:250-311):
+ * offsets x y z and the (already inverted) scales xs ys zs, then the xd x yd samples. */
+int vg_env_add_heightfield_fields(vg_env *env, const float *fields6, size_t xd, size_t yd, const float *data);
 int vg_env_detach(vg_env *env);
 /* Robot::eefk (robots/panda.hh:15447-15552; binding robot_helper.hh:302-305,580): the end
  * effector's transform, row-major 4x4, for configurations q[n][dim].  _device: q and out on the
@@ -208,6 +225,14 @@ int vg_validate_motions_device_noalloc(
 /* Sphere centres and radii of every sphere slot (fine spheres, then each checked link's coarse
  * sphere), out is [n][slots][4].  Replaces Robot::sphere_fk (robots/panda.hh:117-462). */
 int vg_sphere_fk_device(const char *robot, const float *q, size_t n, float *out, void *stream);
+/* Robot::fkcc<rake> (robots/panda.hh:5226-5229; ur5.hh:3218, fetch.hh:17185, baxter.hh:12710) on
+ * caller-given ConfigurationBlocks: q is [n_blocks][lanes][dim] with lanes the environment's
+ * (vg_env_set_mode: 8 or 4); out[b] = 1 when block b is valid, with the reference's block
+ * semantics (a coarse sphere that hits in any lane gates the fine tests of every lane).  Device
+ * form: device buffers on the current GPU, stream-ordered; host form: host buffers,
+ * synchronous. */
+int vg_fkcc_blocks_device(const char *robot, vg_env *env, const float *q, size_t n_blocks, uint8_t *out, void *stream);
+int vg_fkcc_blocks(const char *robot, vg_env *env, const float *q, size_t n_blocks, uint8_t *out);
 
 /* ------------------------------------------------------------------------- checks (host)
  * Same as the device forms with host buffers: copies in, checks, copies out, and waits.

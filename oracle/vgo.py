@@ -43,6 +43,16 @@ def reference_checkout(reference: str | None = None) -> Path | None:
     return ref if (ref / "src" / "impl" / "vamp").is_dir() else None
 
 
+def built_reference_headers() -> Path | None:
+    """The reference's src/impl folder the reference oracle was last built from (None if it has
+    not been built or the folder is gone)."""
+    rec = HERE / "_ref" / "ref_src.txt"
+    if not rec.exists():
+        return None
+    src = Path(rec.read_text().strip())
+    return src if (src / "vamp").is_dir() else None
+
+
 def build_reference(reference: str | None = None) -> Path | None:
     """Compile the reference oracle from the reference checkout (argument or VG_REFERENCE), if
     there is one and the host is x86-64."""

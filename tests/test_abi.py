@@ -73,3 +73,48 @@ def test_errors_are_reported_not_raised_through_the_abi():
     with pytest.raises(vg.VampError):
         env.set_mode(5, 0)
     assert lib.vg_env_add_sphere(None, None) == -1
+
+
+def test_explicit_kind_and_caller_min_distance_are_kept():
+    """vg_env_add_primitive: the object goes to the kind list named, with the caller's
+    min_distance (a converted reference environment's objects already sit in their lists)."""
+    import vamp_gb300 as vg
+
+    env = vg.Environment()
+    cub = [1, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0.1, 0.1, 0.1]  # z-aligned axes, put in the general list
+    env.add_primitive(3, cub, 0.75)
+    env.add_primitive(3, cub, 0.25)
+    env.add_primitive(2, [0, 0, 1, 0.5, 0, 0.5, 0.1, 2.0], 0.5)  # not z-aligned, put in the z list
+    assert [len(env.objects(k)) for k in range(5)] == [0, 0, 1, 2, 0]
+    assert list(env.objects(3)[:, -1]) == [0.25, 0.75]  # kept sorted by min_distance
+    with pytest.raises(ValueError):
+        env.add_primitive(0, cub, 0.0)
+    from vamp_gb300._lib import lib
+
+    f = np.zeros(15, np.float32)
+    assert lib.vg_env_add_primitive(env.handle, 5, f.ctypes.data, 0.0) == -1
+
+
+def test_pointcloud_layout_import_round_trips(port):
+    """vg_env_add_pointcloud_layout takes the reference's tree as built: importing the oracle's
+    tree and reading it back gives the same arrays; inconsistent block ranges are refused."""
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+
+    pts = scenes.surface_pointcloud(9, 1500)
+    lay = port.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS)
+    env = vg.Environment()
+    env.add_pointcloud_layout(lay)
+    back = env.pointcloud_layout(0)
+    for k in ("tests", "aabbs", "aff_starts", "aff", "top"):
+        assert np.array_equal(np.asarray(back[k]), np.asarray(lay[k])), k
+    bad = dict(lay)
+    bad["aff_starts"] = lay["aff_starts"].copy()
+    bad["aff_starts"][3], bad["aff_starts"][4] = bad["aff_starts"][4] + 1, bad["aff_starts"][3]
+    with pytest.raises(vg.VampError):
+        vg.Environment().add_pointcloud_layout(bad)
+    short = dict(lay)
+    short["aff_starts"] = lay["aff_starts"].copy()
+    short["aff_starts"][-1] += 1  # more blocks than given
+    with pytest.raises(vg.VampError):
+        vg.Environment().add_pointcloud_layout(short)

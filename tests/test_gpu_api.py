@@ -44,3 +44,43 @@ def test_predictor_batch_and_autotune_through_the_python_api():
         torch.cuda.synchronize()
         assert np.array_equal(out1.cpu().numpy(), plain)
         assert np.array_equal(out2.cpu().numpy(), vg.ur5.validate_motion_batch(a2, b2, env2))
+
+
+@pytest.mark.parametrize("lanes,sqrt_mode", [(8, 0), (4, 1)])
+def test_fkcc_blocks_are_the_oracles(port, lanes, sqrt_mode):
+    """vg_fkcc_blocks (Robot::fkcc on caller-given blocks, block semantics) against the oracle's
+    fkcc on the same blocks, host and device forms, with a pointcloud in the scene."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+
+    scene = scenes.scene_config1(4)
+    scene["pointclouds"] = [{"points": scenes.surface_pointcloud(8, 3000), "r_min": 0.012, "r_max": 0.08,
+                             "r_point": scenes.POINT_RADIUS}]
+    rb = port.robot("panda")
+    blocks = scenes.configurations(rb.s_m, rb.s_a, 600 * lanes, 19).reshape(600, lanes, 7)
+    env = vg.Environment.from_scene(scene, lanes, sqrt_mode)
+    host = vg.panda.fkcc_blocks(blocks, env)
+    dev = vg.panda.fkcc_blocks(torch.from_numpy(blocks).cuda(), env).cpu().numpy()
+    penv = port.env(scene, sqrt_mode)
+    want = np.array([penv.fkcc_block(rb, np.ascontiguousarray(q)) for q in blocks], np.uint8)
+    assert np.array_equal(host, want)
+    assert np.array_equal(dev, want)
+    assert 0 < want.sum() < len(want)
+
+
+def test_imported_tree_checks_as_the_built_one(port):
+    """A tree imported in the reference layout (vg_env_add_pointcloud_layout) gives the verdicts
+    of the same tree built by vg_env_add_pointcloud."""
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+
+    pts = scenes.surface_pointcloud(10, 5000)
+    built = vg.Environment()
+    built.add_pointcloud(pts, 0.012, 0.08, scenes.POINT_RADIUS)
+    imported = vg.Environment()
+    imported.add_pointcloud_layout(port.capt(pts, 0.012, 0.08, scenes.POINT_RADIUS))
+    rb = port.robot("panda")
+    a, b = scenes.edges(rb.s_m, rb.s_a, 2048, 20)
+    assert np.array_equal(vg.panda.validate_motion_batch(a, b, built, 32), vg.panda.validate_motion_batch(a, b, imported, 32))

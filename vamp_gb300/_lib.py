@@ -58,6 +58,11 @@ def _load() -> ctypes.CDLL:
         "vg_env_pointcloud_layout": ([_p, _i, _p, _p, _p, _p, _p, _p], _i),
         "vg_env_set_mode": ([_p, _i, _i], _i),
         "vg_env_set_schedule": ([_p, _i], _i),
+        "vg_env_add_primitive": ([_p, _i, _p, _f], _i),
+        "vg_env_add_pointcloud_layout": ([_p, _i, _p, _p, _p, _p, _sz, _p, _f, _f, _f], _i),
+        "vg_env_add_heightfield_fields": ([_p, _p, _sz, _sz, _p], _i),
+        "vg_fkcc_blocks_device": ([_s, _p, _p, _sz, _p, _p], _i),
+        "vg_fkcc_blocks": ([_s, _p, _p, _sz, _p], _i),
         "vg_env_count": ([_p, _i, _p], _i),
         "vg_env_get": ([_p, _i, _sz, _p], _i),
         "vg_validate_states_device": ([_s, _p, _p, _sz, _p, _p], _i),
@@ -135,6 +140,11 @@ EXPORTED = (
     "vg_env_pointcloud_layout",
     "vg_env_set_mode",
     "vg_env_set_schedule",
+    "vg_env_add_primitive",
+    "vg_env_add_pointcloud_layout",
+    "vg_env_add_heightfield_fields",
+    "vg_fkcc_blocks_device",
+    "vg_fkcc_blocks",
     "vg_env_count",
     "vg_env_get",
     "vg_validate_states_device",

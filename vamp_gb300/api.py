@@ -163,6 +163,25 @@ class Environment:
         out["aff"] = out["aff"].transpose(1, 0, 2).copy()  # [3][blocks][8], as the oracle dumps it
         return out
 
+    def add_primitive(self, kind: int, fields, min_distance: float) -> None:
+        """One object in an explicit kind list (0 spheres, 1 capsules, 2 z-aligned capsules,
+        3 cuboids, 4 z-aligned cuboids) with the caller's min_distance: for environments converted
+        from the reference's collision::Environment, whose objects already sit in their lists."""
+        f = np.ascontiguousarray(fields, np.float32).reshape(-1)
+        if f.size != [4, 8, 8, 15, 15][kind]:
+            raise ValueError("wrong number of fields for this kind")
+        check(lib.vg_env_add_primitive(self._h, int(kind), _ptr(f), float(min_distance)))
+
+    def add_pointcloud_layout(self, layout: dict) -> None:
+        """A pointcloud tree as the reference built it, in the layout pointcloud_layout returns
+        (nlog2, tests, aabbs, aff_starts, aff [3][blocks][8], top, radii = r_min, r_max, r_point)."""
+        aff = np.ascontiguousarray(np.asarray(layout["aff"], np.float32).transpose(1, 0, 2))  # [blocks][3][8]
+        arr = {k: np.ascontiguousarray(layout[k], np.float32) for k in ("tests", "aabbs", "top")}
+        starts = np.ascontiguousarray(layout["aff_starts"], np.uint32)
+        r = [float(v) for v in layout["radii"]]
+        check(lib.vg_env_add_pointcloud_layout(self._h, int(layout["nlog2"]), _ptr(arr["tests"]), _ptr(arr["aabbs"]),
+                                               _ptr(starts), _ptr(aff), aff.shape[0], _ptr(arr["top"]), *r))
+
     def objects(self, kind: int) -> np.ndarray:
         """Fields of every object of a kind in checking order, min_distance last."""
         n = ctypes.c_size_t()
@@ -293,6 +312,23 @@ class Robot:
         q = np.ascontiguousarray(configurations, np.float32).reshape(-1, self._dim)
         out = np.zeros(len(q), np.uint8) if out is None else out
         check(lib.vg_validate_states(self._b, environment.handle, _ptr(q), len(q), _ptr(out)))
+        return out
+
+    def fkcc_blocks(self, blocks, environment: Environment):
+        """Robot::fkcc (robots/panda.hh:5226-5229) on configuration blocks [n][lanes][dim] (lanes
+        the environment's: 8 or 4) with the reference's block semantics: 1 = the block is valid.
+        numpy in -> numpy out; CUDA tensor in -> CUDA tensor out (current stream)."""
+        if _is_cuda_tensor(blocks):
+            import torch
+
+            q = blocks.contiguous()
+            out = torch.empty(q.shape[0], dtype=torch.uint8, device=q.device)
+            check(lib.vg_fkcc_blocks_device(self._b, environment.handle, q.data_ptr(), q.shape[0], out.data_ptr(),
+                                            torch.cuda.current_stream(q.device).cuda_stream))
+            return out
+        q = np.ascontiguousarray(blocks, np.float32).reshape(-1, environment.lanes, self._dim)
+        out = np.zeros(len(q), np.uint8)
+        check(lib.vg_fkcc_blocks(self._b, environment.handle, _ptr(q), len(q), _ptr(out)))
         return out
 
     def validate_motion_batch(self, starts, goals, environment: Environment, resolution: int | None = None,

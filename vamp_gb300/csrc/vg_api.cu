@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -334,22 +335,48 @@ namespace vg
 
     int sm_count()
     {
-        static int count = 0;
-        if (!count)
+        // per device: grids are sized for the GPU the call runs on
+        constexpr int kDevices = 64;
+        static std::atomic<int> counts[kDevices] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= kDevices)
         {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
-            if (count <= 0)
-            {
-                count = 1;
-            }
+            int c = 0;
+            cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+            return c > 0 ? c : 1;
         }
-        return count;
+        int c = counts[dev].load(std::memory_order_relaxed);
+        if (c <= 0)
+        {
+            cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+            c = c > 0 ? c : 1;
+            counts[dev].store(c, std::memory_order_relaxed);
+        }
+        return c;
     }
 
     int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm)
     {
+        // the attribute and the occupancy of the last few (kernel, device, shared memory, block)
+        // combinations: a single-edge call should not pay two driver queries
+        struct Seen
+        {
+            const void *fn;
+            int dev, smem, block, occ;
+        };
+        static thread_local Seen seen[16] = {};
+        static thread_local int next = 0;
+        int dev = 0;
+        VG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+        for (const Seen &s : seen)
+        {
+            if (s.fn == fn && s.dev == dev && s.smem == smem && s.block == block && s.occ > 0)
+            {
+                *blocks_per_sm = s.occ;
+                return VG_OK;
+            }
+        }
         if (smem > 48 * 1024)
         {
             VG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "cudaFuncSetAttribute");
@@ -360,6 +387,8 @@ namespace vg
         {
             return set_error(VG_ERR_LIMIT, "kernel does not fit on a multiprocessor (environment too large?)");
         }
+        seen[next] = {fn, dev, smem, block, occ};
+        next = (next + 1) % 16;
         *blocks_per_sm = occ;
         return VG_OK;
     }
@@ -586,6 +615,59 @@ int vg_env_add_cuboid(vg_env *env, const float *f)
     return VG_OK;
 }
 
+int vg_env_add_primitive(vg_env *env, int kind, const float *fields, float min_distance)
+{
+    if (!env || !fields || kind < 0 || kind > 4)
+        return set_error(VG_ERR_ARG, "vg_env_add_primitive: kind must be 0..4 and fields non-null");
+    float row[16];
+    std::memcpy(row, fields, sizeof(float) * kFields[kind]);
+    row[kFields[kind]] = min_distance;
+    insert_sorted(env, kind, kFields[kind], row);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_add_pointcloud_layout(vg_env *env, int nlog2, const float *tests, const float *aabbs, const uint32_t *aff_starts,
+                                 const float *aff, size_t n_blocks, const float *top, float r_min, float r_max, float r_point)
+{
+    if (!env || nlog2 < 1 || nlog2 > 30 || !tests || !aabbs || !aff_starts || !top || (n_blocks && !aff) ||
+        !(r_min >= 0.0f) || !(r_max >= r_min) || !(r_point >= 0.0f))
+        return set_error(VG_ERR_ARG, "vg_env_add_pointcloud_layout: bad argument");
+    if (env->clouds.size() >= static_cast<size_t>(kMaxClouds))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud_layout: at most 4 pointclouds per environment");
+    if (n_blocks > 0xffffffffu)
+        return set_error(VG_ERR_LIMIT, "vg_env_add_pointcloud_layout: more than 2^32 - 1 blocks");
+    const size_t leaves = size_t{1} << nlog2;
+    // every leaf's block range must lie inside the blocks given (the queries read [start, end))
+    if (aff_starts[0] > aff_starts[leaves] || aff_starts[leaves] != n_blocks)
+        return set_error(VG_ERR_ARG, "vg_env_add_pointcloud_layout: aff_starts[leaves] must equal n_blocks");
+    for (size_t i = 0; i < leaves; ++i)
+    {
+        if (aff_starts[i] > aff_starts[i + 1])
+            return set_error(VG_ERR_ARG, "vg_env_add_pointcloud_layout: aff_starts must not decrease");
+    }
+    try
+    {
+        CaptHost c;
+        c.nlog2 = nlog2;
+        c.tests.assign(tests, tests + (leaves - 1));
+        c.aabbs.assign(aabbs, aabbs + leaves * 6);
+        c.aff_starts.assign(aff_starts, aff_starts + leaves + 1);
+        c.aff.assign(aff, aff + n_blocks * 24);
+        std::memcpy(c.top, top, sizeof(c.top));
+        c.r_min = r_min;
+        c.r_max = r_max;
+        c.r_point = r_point;
+        env->clouds.push_back(std::move(c));
+    }
+    catch (...)
+    {
+        return set_error(VG_ERR_NOMEM, "vg_env_add_pointcloud_layout: out of host memory");
+    }
+    env->dirty = true;
+    return VG_OK;
+}
+
 int vg_env_add_pointcloud(vg_env *env, const float *xyz, size_t n, float r_min, float r_max, float r_point)
 {
     if (!env || !xyz || n < 2 || !(r_min >= 0.0f) || !(r_max >= r_min) || !(r_point >= 0.0f))
@@ -774,6 +856,30 @@ int vg_env_add_heightfield(vg_env *env, const float *centre, const float *scale,
     v.xs = 1.0f / scale[0];
     v.ys = 1.0f / scale[1];
     v.zs = 1.0f / scale[2];
+    v.xd = static_cast<int>(xd);
+    v.yd = static_cast<int>(yd);
+    v.id = env->n_added++;
+    env->hf.push_back(v);
+    env->hf_data.emplace_back(data, data + xd * yd);
+    env->dirty = true;
+    return VG_OK;
+}
+
+int vg_env_add_heightfield_fields(vg_env *env, const float *fields6, size_t xd, size_t yd, const float *data)
+{
+    if (!env || !fields6 || !data || xd == 0 || yd == 0)
+        return set_error(VG_ERR_ARG, "vg_env_add_heightfield_fields: null argument or empty grid");
+    if (env->hf.size() >= static_cast<size_t>(kMaxHeightfields))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_heightfield_fields: at most 8 heightfields per environment");
+    if (xd >= (size_t{1} << 24) || yd >= (size_t{1} << 24) || xd * yd >= (size_t{1} << 24))
+        return set_error(VG_ERR_LIMIT, "vg_env_add_heightfield_fields: at most 2^24 samples (cell indices are exact in FP32)");
+    HeightView v{};
+    v.x = fields6[0];
+    v.y = fields6[1];
+    v.z = fields6[2];
+    v.xs = fields6[3];
+    v.ys = fields6[4];
+    v.zs = fields6[5];
     v.xd = static_cast<int>(xd);
     v.yd = static_cast<int>(yd);
     v.id = env->n_added++;
@@ -993,6 +1099,53 @@ int vg_validate_states(const char *robot, vg_env *env, const float *q, size_t n,
     if (int rc = vg_validate_states_device(robot, env, dq, n, dout, nullptr))
         return rc;
     VG_CUDA(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, 0), "copy verdicts");
+    VG_CUDA(cudaStreamSynchronize(0), "synchronize");
+    return VG_OK;
+}
+
+int vg_fkcc_blocks_device(const char *robot, vg_env *env, const float *q, size_t n_blocks, uint8_t *out, void *stream)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n_blocks && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_fkcc_blocks_device: bad argument");
+    if (n_blocks > (size_t{1} << 40))
+        return set_error(VG_ERR_LIMIT, "vg_fkcc_blocks_device: more than 2^40 blocks");
+    if (n_blocks == 0)
+        return VG_OK;
+    if (int rc = commit(env))
+        return rc;
+    const int which = env->lanes == 8 ? 0 : 1;
+    const bool ext = env->extended();
+    const int smem = static_cast<int>(staged_f4(static_cast<int>(env->image_f4)) * sizeof(float4)) + r->stage_floats * kBlock * 4;
+    int occ = 0;
+    if (int rc = prepare_kernel(ext ? r->blocks_ext_fn[which] : r->blocks_fn[which], smem, kBlock, &occ))
+        return rc;
+    const long long per_block = (kBlock / 32) * (32 / env->lanes);  // configuration blocks per thread block
+    const long long want = (static_cast<long long>(n_blocks) + per_block - 1) / per_block;
+    const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
+    StatesParams p{q, static_cast<long long>(n_blocks), out, env_device(env)};
+    VG_CUDA((ext ? r->blocks_ext[which] : r->blocks[which])(p, grid, kBlock, smem, static_cast<cudaStream_t>(stream)),
+            "blocks kernel launch");
+    return VG_OK;
+}
+
+int vg_fkcc_blocks(const char *robot, vg_env *env, const float *q, size_t n_blocks, uint8_t *out)
+{
+    const RobotOps *r = find_robot(robot);
+    if (!r || !env || (n_blocks && (!q || !out)))
+        return set_error(VG_ERR_ARG, "vg_fkcc_blocks: bad argument");
+    if (n_blocks == 0)
+        return VG_OK;
+    const size_t qb = n_blocks * static_cast<size_t>(env->lanes) * r->dim * sizeof(float);
+    const size_t qa = (qb + 255) & ~size_t(255);
+    if (int rc = ensure_stage(env, qa + n_blocks))
+        return rc;
+    float *dq = static_cast<float *>(env->d_stage);
+    uint8_t *dout = static_cast<uint8_t *>(env->d_stage) + qa;
+    VG_CUDA(cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, 0), "copy configuration blocks");
+    if (int rc = vg_fkcc_blocks_device(robot, env, dq, n_blocks, dout, nullptr))
+        return rc;
+    VG_CUDA(cudaMemcpyAsync(out, dout, n_blocks, cudaMemcpyDeviceToHost, 0), "copy verdicts");
     VG_CUDA(cudaStreamSynchronize(0), "synchronize");
     return VG_OK;
 }

@@ -24,6 +24,12 @@ namespace vg
         const float *s_a;
         cudaError_t (*states)(const StatesParams &, int grid, int block, int smem, cudaStream_t);
         const void *states_fn;
+        // caller-given blocks of 8 (index 0) or 4 (index 1) configurations (Robot::fkcc), and the
+        // extended form
+        cudaError_t (*blocks[2])(const StatesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *blocks_fn[2];
+        cudaError_t (*blocks_ext[2])(const StatesParams &, int grid, int block, int smem, cudaStream_t);
+        const void *blocks_ext_fn[2];
         // edges: index 0 = 8-lane blocks, 1 = 4-lane blocks
         cudaError_t (*edges[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_fn[2];

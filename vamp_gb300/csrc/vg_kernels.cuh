@@ -216,6 +216,41 @@ namespace vg
         }
     }
 
+    // ------------------------------------------------------------------------------ blocks
+
+    // Robot::fkcc on caller-given blocks of W configurations (robots/panda.hh:5226-5229): each
+    // W-lane segment is one ConfigurationBlock<W>, with the reference's block semantics (coarse
+    // gates and loop exits decided for the whole block); out[b] = 1 when block b is valid.  q is
+    // [n][W][dim].  kExt: the extended checks (heightfields, fkcc_attach).
+    template <typename Robot, int W, bool kExt = false>
+    __global__ void __launch_bounds__(128, VG_MIN_BLOCKS) blocks_kernel(StatesParams p)
+    {
+        extern __shared__ float4 smem[];
+        const EnvView ev = stage_env(p.env, smem);
+        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
+        constexpr int D = Robot::kDim;
+        constexpr int S = 32 / W;  // blocks per warp
+        const int lane = threadIdx.x & 31;
+        const long long stride = static_cast<long long>(gridDim.x) * (blockDim.x >> 5) * S;
+        for (long long base = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * S; base < p.n;
+             base += stride)
+        {
+            const long long blk = base + lane / W;
+            const bool in = blk < p.n;
+            float q[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                q[d] = in ? p.q[(blk * W + lane % W) * D + d] : 0.0f;
+            }
+            const unsigned alive = run_fkcc<Robot, W, true, kExt>(ev, q, __ballot_sync(kFull, in), stage);
+            if (in && lane % W == 0)
+            {
+                p.out[blk] = static_cast<uint8_t>((alive >> lane) & 1u);
+            }
+        }
+    }
+
     // ------------------------------------------------------------------------------- edges
 
     struct EdgesParams

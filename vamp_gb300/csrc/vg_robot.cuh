@@ -14,6 +14,13 @@ namespace vg
     }
 
     template <typename R, int W, bool kExt = false>
+    cudaError_t launch_blocks(const StatesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        blocks_kernel<R, W, kExt><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
+    template <typename R, int W, bool kExt = false>
     cudaError_t launch_edges(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
         edges_kernel<R, W, kExt><<<grid, block, smem, s>>>(p);
@@ -92,6 +99,14 @@ namespace vg
         o.s_a = R::kScaleA;
         o.states = &launch_states<R>;
         o.states_fn = reinterpret_cast<const void *>(&states_kernel<R>);
+        o.blocks[0] = &launch_blocks<R, 8>;
+        o.blocks[1] = &launch_blocks<R, 4>;
+        o.blocks_fn[0] = reinterpret_cast<const void *>(&blocks_kernel<R, 8>);
+        o.blocks_fn[1] = reinterpret_cast<const void *>(&blocks_kernel<R, 4>);
+        o.blocks_ext[0] = &launch_blocks<R, 8, true>;
+        o.blocks_ext[1] = &launch_blocks<R, 4, true>;
+        o.blocks_ext_fn[0] = reinterpret_cast<const void *>(&blocks_kernel<R, 8, true>);
+        o.blocks_ext_fn[1] = reinterpret_cast<const void *>(&blocks_kernel<R, 4, true>);
         o.edges[0] = &launch_edges<R, 8>;
         o.edges[1] = &launch_edges<R, 4>;
         o.edges_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8>);
