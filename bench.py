@@ -231,6 +231,15 @@ def fp32_peak_tflops(device_props, sm_mhz: float | None):
     return sms * 128 * 2 * mhz * 1e6 / 1e12, mhz, sms
 
 
+# The compiled reference's own code (its AVX2 build) on the benchmark workload, timed on an x86-64
+# host by oracle/time_reference.py: the GPU machine is an Arm machine without the reference checkout,
+# so its CPU baseline is the C restatement (kind "port"); this record states the reference's rate
+# beside it.
+REFERENCE_X86 = {"edges_per_s": 387820.0, "threads": 8, "edges_per_s_one_thread": 67543.0,
+                 "host": "Intel Xeon @ 2.70 GHz (8 threads)", "build": "x86-64 AVX2, 8 lanes",
+                 "how": "python oracle/time_reference.py (best of 5 passes over the 65,536 edges)"}
+
+
 def cpu_baseline(scene, a, b, budget_s: float = 10.0):
     """The reference's algorithm on the host cores: the compiled reference when it loads here,
     else the CPU oracle.  Bounded sample: whole passes over a slice of the edges until about
@@ -267,8 +276,11 @@ def cpu_baseline(scene, a, b, budget_s: float = 10.0):
         fn(a[:n], b[:n])
         done += n
     elapsed = time.perf_counter() - t0
-    return {"value": done / elapsed, "unit": "edges/s", "cores": threads, "kind": kind,
-            "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
+    out = {"value": done / elapsed, "unit": "edges/s", "cores": threads, "kind": kind,
+           "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
+    if kind == "port":
+        out["reference_x86"] = REFERENCE_X86
+    return out
 
 
 def autotune(robot: str, env, a, b, resolution: int, stream, sample: int = 65536) -> dict:
@@ -609,7 +621,8 @@ def run_reference(args, world, rank):
         "dtype": "f32",
         "data": "synthetic (seeded scene and edges)",
         "config": {"workload": WORKLOAD, "edges": N_EDGES, "resolution": RESOLUTION, "l2": "host CPU run"},
-        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": res["cores"], "kind": res["kind"], "sample": res["sample"]},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": res["cores"], "kind": res["kind"], "sample": res["sample"],
+                         **({"reference_x86": res["reference_x86"]} if "reference_x86" in res else {})},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

@@ -209,6 +209,10 @@ int vg_validate_motions_device(
  * exit.  Requirements: env already uploaded to the current device by an earlier ordinary check
  * call and unchanged since (VG_ERR_STATE otherwise); n <= 2^31 - 1 (VG_ERR_LIMIT).  The first
  * call on each device looks up the array's device address: make it before any stream capture.
+ * Under CUDA's lazy module loading the driver loads a kernel the first time it runs, which may
+ * allocate: let the earlier ordinary call be a vg_validate_motions_device with the same robot,
+ * environment settings and schedule (so the same kernel is already loaded), or run with
+ * CUDA_MODULE_LOADING=EAGER.
  * All calls share the array (the counter is cleared on `stream` before each launch): calls whose
  * kernels overlap on the GPU race, so issue them on one stream or wait between them. */
 int vg_validate_motions_device_noalloc(
@@ -303,8 +307,15 @@ int vg_mlp_infer_device(vg_mlp *m, const float *q, size_t n, float *p, void *str
 int vg_mlp_score_edges_device(vg_mlp *m, const float *a, const float *b, size_t n, int probes, float *scores,
                               void *stream);
 
-/* VG_OK, or VG_ERR_CUDA if a tensor-core kernel of m gave up waiting for its MMAs (synchronous). */
+/* VG_OK, or VG_ERR_CUDA if a tensor-core kernel of m gave up waiting for its MMAs since the last
+ * report (synchronous).  A kernel that gives up sets the flag, waits (with the default limit) for
+ * the MMAs it issued, frees its tensor memory and returns; later kernels of m then do nothing
+ * until this call reports the flag, which clears it. */
 int vg_mlp_error(vg_mlp *m);
+/* How many times m's tensor-core kernels poll an MMA-completion barrier before they give up
+ * (negative: the default, 2^22; 0: give up at once, which the failure tests use).  The wait for
+ * MMAs still in flight before tensor memory is released always uses the default. */
+int vg_mlp_set_wait_limit(vg_mlp *m, long long polls);
 
 /* validate_motion verdicts (those of vg_validate_motions_device, bit for bit) with each edge's
  * blocks checked in the order the scores rank them: block 0 first, then blocks by the largest

@@ -13,7 +13,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_edge_check_matches_the_ordinary_entry_point_twice():
+# (schedule, extended): the robot's default schedule and every other one; and an environment with
+# a heightfield, which runs the extended segment-per-edge kernel
+CASES = [(None, False), (0, False), (1, False), (2, False), (3, False), (None, True)]
+
+
+@pytest.mark.parametrize("schedule,extended", CASES)
+def test_noalloc_edge_check_matches_the_ordinary_entry_point_twice(schedule, extended):
     import torch
 
     import vamp_gb300 as vg
@@ -21,7 +27,12 @@ def test_noalloc_edge_check_matches_the_ordinary_entry_point_twice():
     from vamp_gb300._lib import lib
 
     rb = vg.panda
-    env = vg.Environment.from_scene(scenes.scene_config1(1))
+    scene = scenes.scene_config1(1)
+    if extended:
+        scene["heightfields"] = [scenes.heightfield(6)]
+    env = vg.Environment.from_scene(scene)
+    if schedule is not None:
+        env.set_schedule(schedule)
     a, b = scenes.edges(rb.s_m, rb.s_a, 16384, 606)
     da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     stream = torch.cuda.current_stream().cuda_stream

@@ -58,6 +58,7 @@ def _load() -> ctypes.CDLL:
         "vg_env_pointcloud_layout": ([_p, _i, _p, _p, _p, _p, _p, _p], _i),
         "vg_env_set_mode": ([_p, _i, _i], _i),
         "vg_env_set_schedule": ([_p, _i], _i),
+        "vg_mlp_set_wait_limit": ([_p, ctypes.c_longlong], _i),
         "vg_env_add_primitive": ([_p, _i, _p, _f], _i),
         "vg_env_add_pointcloud_layout": ([_p, _i, _p, _p, _p, _p, _sz, _p, _f, _f, _f], _i),
         "vg_env_add_heightfield_fields": ([_p, _p, _sz, _sz, _p], _i),
@@ -166,6 +167,7 @@ EXPORTED = (
     "vg_mlp_infer_device",
     "vg_mlp_score_edges_device",
     "vg_mlp_error",
+    "vg_mlp_set_wait_limit",
     "vg_validate_motions_scored_device",
     "vg_validate_motions_learned_device",
     "vg_autotune_motions",

@@ -71,9 +71,6 @@ def _defines() -> list[str]:
     # VG_DEFAULT_LOOPED_ENV=1: the default edge kernel runs the environment section as loops
     if os.environ.get("VG_DEFAULT_LOOPED_ENV") == "1":
         out.append("-DVG_DEFAULT_LOOPED_ENV=1")
-    # VG_LOCKSTEP=1: the default same-edge kernel keeps a block's warps in step
-    if os.environ.get("VG_LOCKSTEP") == "1":
-        out.append("-DVG_LOCKSTEP")
     w = os.environ.get("VG_CAPT_SHARED_WEIGHT")
     if w:
         out.append(f"-DVG_CAPT_SHARED_WEIGHT={int(w)}")

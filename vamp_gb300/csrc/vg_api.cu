@@ -358,8 +358,10 @@ namespace vg
 
     int prepare_kernel(const void *fn, int smem, int block, int *blocks_per_sm)
     {
-        // the attribute and the occupancy of the last few (kernel, device, shared memory, block)
-        // combinations: a single-edge call should not pay two driver queries
+        // The occupancy of the last few (kernel, device, shared memory, block) combinations is
+        // kept, so that a single-edge call does not pay the driver's occupancy query.  The
+        // kernel's dynamic shared-memory limit is set on every call: it is one value per kernel,
+        // which a call with a smaller environment lowers.
         struct Seen
         {
             const void *fn;
@@ -373,9 +375,21 @@ namespace vg
         {
             if (s.fn == fn && s.dev == dev && s.smem == smem && s.block == block && s.occ > 0)
             {
+                if (smem > 48 * 1024)
+                {
+                    VG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "cudaFuncSetAttribute");
+                }
                 *blocks_per_sm = s.occ;
                 return VG_OK;
             }
+        }
+        int smem_max = 0;
+        VG_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared-memory limit");
+        if (smem > smem_max)
+        {
+            return set_error(VG_ERR_LIMIT, "the environment and the robot's staging need " + std::to_string(smem) +
+                                               " bytes of shared memory per block, more than the GPU's " +
+                                               std::to_string(smem_max) + " (too many primitives)");
         }
         if (smem > 48 * 1024)
         {

@@ -821,122 +821,6 @@ namespace vg
         }
     }
 
-    // The same-edge schedule with the four warps of a block kept in step: one barrier per check
-    // iteration, so that the block's warps run the same part of the check at about the same time
-    // and share its instruction-cache lines.  Same blocks, same order, same verdicts and block
-    // counts as edges_grouped_kernel (reference block order only).
-    template <typename Robot, int W, int kMinBlocks = VG_MIN_BLOCKS>
-    __global__ void __launch_bounds__(128, kMinBlocks) edges_lockstep_kernel(EdgesParams p)
-    {
-        extern __shared__ float4 smem[];
-        const EnvView ev = stage_env(p.env, smem);
-        float *const stage = reinterpret_cast<float *>(smem + staged_f4(p.env.n_f4)) + threadIdx.x;
-        constexpr int D = Robot::kDim;
-        constexpr int S = 32 / W;
-        const int lane = threadIdx.x & 31;
-        const int seg = lane / W;
-        const int sl = lane % W;
-        const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
-
-        int e = -1;       // this warp's edge (-1: none; -2: the queue is empty)
-        int n = 0, i0 = 0;
-        float q[D], bs[D];
-        for (;;)
-        {
-            if (e == -1)
-            {
-                unsigned got = 0;
-                if (lane == 0)
-                {
-                    got = atomicAdd(p.head, 1u);
-                }
-                got = __shfl_sync(kFull, got, 0);
-                if (got >= static_cast<unsigned>(p.n))
-                {
-                    e = -2;
-                }
-                else
-                {
-                    e = static_cast<int>(got);
-                    float v[D];
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                    {
-                        const float av = p.a[static_cast<long long>(e) * D + d];
-                        v[d] = p.dist ? p.b[static_cast<long long>(e) * D + d]
-                                      : __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
-                        q[d] = __fmaf_rn(v[d], pct, av);
-                    }
-                    const float len = p.dist ? p.dist[e] : edge_length<D>(v);
-                    const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
-                    const float nf = ceilf(t);
-                    n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
-                    const float denom = static_cast<float>(W * n);
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                    {
-                        bs[d] = __fdiv_rn(v[d], denom);
-                    }
-                    for (int k = 0; k < seg; ++k)
-                    {
-#pragma unroll
-                        for (int d = 0; d < D; ++d)
-                        {
-                            q[d] = __fsub_rn(q[d], bs[d]);
-                        }
-                    }
-                    i0 = 0;
-                }
-            }
-            // every warp of the block reaches this barrier once per iteration
-            if (__syncthreads_and(e == -2))
-            {
-                break;
-            }
-            if (e < 0)
-            {
-                continue;
-            }
-            const bool active = i0 + seg < n;
-            const unsigned mask = __ballot_sync(kFull, active);
-            const unsigned alive = run_fkcc<Robot, W>(ev, q, mask, stage);
-            const unsigned dead = mask & ~alive;
-            int done = 0, verdict = 1, checked = n;
-            if (dead)
-            {
-                verdict = 0;
-                checked = i0 + (__ffs(dead) - 1) / W + 1;
-                done = 1;
-            }
-            else
-            {
-                i0 += S;
-                done = i0 >= n;
-#pragma unroll 1
-                for (int k = 0; k < S; ++k)
-                {
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                    {
-                        q[d] = __fsub_rn(q[d], bs[d]);
-                    }
-                }
-            }
-            if (done)
-            {
-                if (lane == 0)
-                {
-                    p.out[e] = static_cast<uint8_t>(verdict);
-                    if (p.blocks)
-                    {
-                        p.blocks[e] = checked;
-                    }
-                }
-                e = -1;
-            }
-        }
-    }
-
     // ----------------------------------------------------------------------- debug reports
     //
     // Robot::fkcc_debug (robots/panda.hh:468) for a batch of configurations, from their sphere

@@ -28,6 +28,9 @@ namespace vg
         const float *bias;       // [N]
         int M, N, K;
         int *err;                // set to 1 if a wait gave up
+        // polls of an MMA-completion barrier before the kernel gives up (the wait for MMAs still
+        // in flight before the tensor memory is released always uses kWaitLimit)
+        uint32_t wait_limit = kWaitLimit;
     };
 
     // D[M x N] = A[M x K] B[N x K]^T.  One CTA of 128 threads per 128-row tile; N in 16..256 (a
@@ -102,7 +105,7 @@ namespace vg
                 }
                 tc::mma_commit(&bar);
             }
-            ok = tc::mbar_wait(&bar, phase, kWaitLimit);
+            ok = tc::mbar_wait(&bar, phase, p.wait_limit);
             phase ^= 1u;
             if (!__syncthreads_and(ok))
             {
@@ -361,6 +364,7 @@ struct vg_mlp
     __nv_bfloat16 *x = nullptr, *h1 = nullptr, *h2 = nullptr, *dh2 = nullptr, *dh1 = nullptr, *t0 = nullptr, *t1 = nullptr;
     float *f32 = nullptr, *z = nullptr, *p = nullptr, *dz = nullptr, *loss = nullptr;
     int *err = nullptr;
+    uint32_t wait_limit = vg::kWaitLimit;  // vg_mlp_set_wait_limit
     float *scores = nullptr;  // probe scores of the last learned edge check
     size_t scores_cap = 0;
 
@@ -423,8 +427,10 @@ namespace vg
     {
         features_kernel<<<(rows * m->kin + 255) / 256, 256, 0, s>>>(q, n, m->dim, m->kin, m->x, rows);
         GemmParams g1{m->x, m->w1b, nullptr, m->h1, m->B1(), rows, kHidden, m->kin, m->err};
+        g1.wait_limit = m->wait_limit;
         cudaError_t e = gemm_bf16(g1, kEpiBiasReluBf16, s);
         GemmParams g2{m->h1, m->w2b, nullptr, m->h2, m->B2(), rows, kHidden, kHidden, m->err};
+        g2.wait_limit = m->wait_limit;
         if (e == cudaSuccess)
             e = gemm_bf16(g2, kEpiBiasReluBf16, s);
         if (e == cudaSuccess)
@@ -450,9 +456,11 @@ namespace vg
         transpose_kernel<<<dim3(kHidden / 32, rows / 32), tb, 0, s>>>(m->dh2, m->t0, rows, kHidden);
         transpose_kernel<<<dim3(kHidden / 32, rows / 32), tb, 0, s>>>(m->h1, m->t1, rows, kHidden);
         GemmParams gw2{m->t0, m->t1, m->G(gr, m->W2()), nullptr, nullptr, kHidden, kHidden, rows, m->err};
+        gw2.wait_limit = m->wait_limit;
         cudaError_t e = gemm_bf16(gw2, kEpiStoreF32, s);
         // dH1 = (dH2 W2) * (H1 > 0): B operand is W2^T as [i][j]
         GemmParams gh1{m->dh2, m->w2tb, m->f32, nullptr, nullptr, rows, kHidden, kHidden, m->err};
+        gh1.wait_limit = m->wait_limit;
         if (e == cudaSuccess)
             e = gemm_bf16(gh1, kEpiStoreF32, s);
         if (e != cudaSuccess)
@@ -463,6 +471,7 @@ namespace vg
         transpose_kernel<<<dim3(kHidden / 32, rows / 32), tb, 0, s>>>(m->dh1, m->t0, rows, kHidden);
         transpose_kernel<<<dim3((m->kin + 31) / 32, rows / 32), tb, 0, s>>>(m->x, m->t1, rows, m->kin);
         GemmParams gw1{m->t0, m->t1, m->G(gr, m->W1()), nullptr, nullptr, kHidden, m->kin, rows, m->err};
+        gw1.wait_limit = m->wait_limit;
         e = gemm_bf16(gw1, kEpiStoreF32, s);
         if (e != cudaSuccess)
             return set_error(VG_ERR_CUDA, std::string("MLP backward: ") + cudaGetErrorString(e));
@@ -715,6 +724,7 @@ namespace vg
         float *out;               // [rows]
         int probability;          // 1: sigmoid(z), 0: z
         int *err;
+        uint32_t wait_limit = kWaitLimit;  // as GemmParams::wait_limit
     };
 
     template <int KIN>
@@ -823,7 +833,7 @@ namespace vg
                                  tc::smem_desc(w0 + kk * 256, 128, (KIN / 8) * 128), idesc, kk > 0);
                 tc::mma_commit(&bar);
             }
-            ok = tc::mbar_wait(&bar, phase, kWaitLimit);
+            ok = tc::mbar_wait(&bar, phase, p.wait_limit);
             phase ^= 1u;
             if (!__syncthreads_and(ok))
             {
@@ -859,7 +869,7 @@ namespace vg
                                  tc::smem_desc(w0 + kk * 256, 128, (kHidden / 8) * 128), idesc, kk > 0);
                 tc::mma_commit(&bar);
             }
-            ok = tc::mbar_wait(&bar, phase, kWaitLimit);
+            ok = tc::mbar_wait(&bar, phase, p.wait_limit);
             phase ^= 1u;
             if (!__syncthreads_and(ok))
             {
@@ -905,6 +915,7 @@ namespace vg
         if (rows == 0)
             return VG_OK;
         InferParams ip{a, b, probes, rows, m->dim, m->w1b, m->w2b, m->B1(), m->B2(), m->W3(), m->B3(), out, probability, m->err};
+        ip.wait_limit = m->wait_limit;
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -957,7 +968,22 @@ int vg_mlp_error(vg_mlp *m)
 {
     if (!m)
         return set_error(VG_ERR_ARG, "vg_mlp_error: null");
-    return mlp_check_err(m);
+    const int rc = mlp_check_err(m);
+    if (rc != VG_OK)
+    {
+        // reported once: later calls on this handle run again
+        cudaMemset(m->err, 0, sizeof(int));
+        cudaDeviceSynchronize();
+    }
+    return rc;
+}
+
+int vg_mlp_set_wait_limit(vg_mlp *m, long long polls)
+{
+    if (!m || polls > 0x7fffffffLL)
+        return set_error(VG_ERR_ARG, "vg_mlp_set_wait_limit: polls must be at most 2^31 - 1 (negative: the default)");
+    m->wait_limit = polls < 0 ? kWaitLimit : static_cast<uint32_t>(polls);
+    return VG_OK;
 }
 
 }  // extern "C"

@@ -52,13 +52,6 @@ namespace vg
         return cudaGetLastError();
     }
 
-    template <typename R, int W>
-    cudaError_t launch_edges_lockstep(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
-    {
-        edges_lockstep_kernel<R, W><<<grid, block, smem, s>>>(p);
-        return cudaGetLastError();
-    }
-
     template <typename R>
     cudaError_t launch_debug_self(const float *spheres, long long n, uint8_t *out, cudaStream_t s)
     {
@@ -111,17 +104,10 @@ namespace vg
         o.edges[1] = &launch_edges<R, 4>;
         o.edges_fn[0] = reinterpret_cast<const void *>(&edges_kernel<R, 8>);
         o.edges_fn[1] = reinterpret_cast<const void *>(&edges_kernel<R, 4>);
-#ifdef VG_LOCKSTEP
-        o.edges_grouped[0] = &launch_edges_lockstep<R, 8>;
-        o.edges_grouped[1] = &launch_edges_lockstep<R, 4>;
-        o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_lockstep_kernel<R, 8>);
-        o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_lockstep_kernel<R, 4>);
-#else
         o.edges_grouped[0] = &launch_edges_grouped<R, 8, false>;
         o.edges_grouped[1] = &launch_edges_grouped<R, 4, false>;
         o.edges_grouped_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false>);
         o.edges_grouped_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, false>);
-#endif
         o.edges_wide[0] = &launch_edges_grouped<R, 8, false, VG_MIN_BLOCKS_WIDE, true>;
         o.edges_wide[1] = &launch_edges_grouped<R, 4, false, VG_MIN_BLOCKS_WIDE, true>;
         o.edges_wide_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, false, VG_MIN_BLOCKS_WIDE, true>);

@@ -617,23 +617,24 @@ def gen_cuda(model: dict) -> str:
             v = kin.sphere_in_frame(l, p)[1]
             offs.append(f"{{{lit32(em0.const(float(v[0])))}, {lit32(em0.const(float(v[1])))}, {lit32(em0.const(float(v[2])))}, {lit32(r)}}}")
         w(f"    __constant__ float4 {pre}SlotOff[{len(slots)}] = {{{', '.join(offs)}}};")
-        # tables of the table-driven form: only where that form is compiled
-        tab_if = "#ifndef VG_STAGED_ALL" if tabled else "#if 0"
-        stg_if = "#ifdef VG_STAGED_ALL" if tabled else "#if 1"
+        # tables of the table-driven form: only for the robots that compile that form (and
+        # only while VG_STAGED_ALL does not switch them to the staged form)
         w(f"    __constant__ int {pre}EnvStart[{len(env_start)}] = {{{', '.join(map(str, env_start))}}};")
-        w(tab_if)
-        w(f"    __constant__ int {pre}EnvCoarse[{len(model['env_checks'])}] = {{{', '.join(str(coarse_slot[e['link']]) for e in model['env_checks'])}}};")
-        w("#endif")
+        if tabled:
+            w("#ifndef VG_STAGED_ALL")
+            w(f"    __constant__ int {pre}EnvCoarse[{len(model['env_checks'])}] = {{{', '.join(str(coarse_slot[e['link']]) for e in model['env_checks'])}}};")
+            w("#endif")
         w(f"    __constant__ int {pre}EnvFine[{len(env_fine)}] = {{{', '.join(map(str, env_fine))}}};")
-        w(tab_if)
-        w(f"    // per link pair: coarse slot A, coarse slot B, start of A's and B's fine lists, their sizes")
-        w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
-        w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
-        w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
-        env_of = {e["link"]: k for k, e in enumerate(model["env_checks"])}
-        w(f"    // per link pair: environment-check index of link A's and link B's coarse sphere")
-        w(f"    __constant__ int2 {pre}SelfEnvIdx[{len(self_rows)}] = {{{', '.join('{%d, %d}' % (env_of[e['links'][0]], env_of[e['links'][1]]) for e in model['self_checks'])}}};")
-        w("#endif")
+        if tabled:
+            w("#ifndef VG_STAGED_ALL")
+            w(f"    // per link pair: coarse slot A, coarse slot B, start of A's and B's fine lists, their sizes")
+            w(f"    __constant__ int4 {pre}SelfRow[{len(self_rows)}] = {{{', '.join('{%d, %d, %d, %d}' % r[:4] for r in self_rows)}}};")
+            w(f"    __constant__ int2 {pre}SelfLen[{len(self_rows)}] = {{{', '.join('{%d, %d}' % r[4:] for r in self_rows)}}};")
+            w(f"    __constant__ int {pre}SelfList[{len(self_list)}] = {{{', '.join(map(str, self_list))}}};")
+            env_of = {e["link"]: k for k, e in enumerate(model["env_checks"])}
+            w(f"    // per link pair: environment-check index of link A's and link B's coarse sphere")
+            w(f"    __constant__ int2 {pre}SelfEnvIdx[{len(self_rows)}] = {{{', '.join('{%d, %d}' % (env_of[e['links'][0]], env_of[e['links'][1]]) for e in model['self_checks'])}}};")
+            w("#endif")
         cull = load_cull(name)
         live_start, live_pairs = [0], []
         for ci, e in enumerate(model["self_checks"]):
@@ -650,7 +651,9 @@ def gen_cuda(model: dict) -> str:
         w(f"    // links checked against an attachment (fkcc_attach): coarse slot, fine range; fine slots")
         w(f"    __device__ const int4 {pre}AttachLink[{max(1, len(arows))}] = {{{', '.join('{%d, %d, %d, 0}' % r for r in arows) or '{0, 0, 0, 0}'}}};")
         w(f"    __device__ const int {pre}AttachFine[{max(1, len(afine))}] = {{{', '.join(map(str, afine)) or '0'}}};")
-        w(stg_if)
+        # tables of the staged form: every robot's default except the table-driven ones
+        if tabled:
+            w("#ifdef VG_STAGED_ALL")
         w(f"    __constant__ int2 {pre}FullPair[{max(1, len(all_pairs))}] = {{{', '.join('{%d, %d}' % p for p in all_pairs) or '{0, 0}'}}};")
         if True:
             lay = stage_layout(model, kin, load_cull(name))
@@ -695,7 +698,8 @@ def gen_cuda(model: dict) -> str:
             w(f"    __constant__ int4 {pre}SelfJoint[{len(cb_checks)}] = {{{', '.join('{%d, %d, %d, 0}' % ((jp[c[0][0]], jp[c[0][1]], c[0][2]) if c[0][2] >= 0 else (0, 0, -1)) for c in cb_checks)}}};")
             w(f"    __constant__ float4 {pre}SelfBox[{len(cb_checks)}] = {{{', '.join(box(c[1]) for c in cb_checks)}}};")
             w(f"    __constant__ float4 {pre}LiveBox[{max(1, len(cb_pairs))}] = {{{', '.join(box(p_) for p_ in cb_pairs) or box((0, 0, 0, 0))}}};")
-        w("#endif")
+        if tabled:
+            w("#endif")
         w("")
 
     w("struct %s" % S)
