@@ -781,7 +781,7 @@ def run_gpu(args, world, rank, local):
     plain_blocks = torch.empty(N_EDGES, dtype=torch.int32, device=dev)  # untimed: the block counts
     check(lib.vg_validate_motions_device(b"panda", env.handle, a.data_ptr(), b.data_ptr(), N_EDGES, RESOLUTION,
                                          out.data_ptr(), plain_blocks.data_ptr(), stream.cuda_stream))
-    learned = None if args.no_learned else measure_learned(args, env, a, b, out, stream, flush, dev)
+    learned = None if args.no_learned else measure_learned(args, env, a, b, out, stream, flush, dev, probes=args.probes)
 
     # end to end through the C ABI with host buffers
     pa = torch.empty(a_np.shape, dtype=torch.float32, pin_memory=True).numpy()
@@ -858,6 +858,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-order measurement")
     ap.add_argument("--labels", type=int, default=2 << 20, help="exact-checker labels the learned order trains on")
+    ap.add_argument("--probes", type=int, default=8, help="states per edge the learned order scores")
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
                          "2 warp per edge with the register-rich build, 3 as 2 with free segments starting the next edge")

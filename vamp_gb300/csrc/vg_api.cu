@@ -468,7 +468,18 @@ namespace vg
         const long long want = (static_cast<long long>(m.n) + per_block - 1) / per_block;
         const int grid = static_cast<int>(std::min<long long>(want, static_cast<long long>(sm_count()) * occ));
         EdgesParams p{m.a, m.b, static_cast<int>(m.n), m.resolution, m.out, m.blocks, m.counter, env_device(env), m.scores, m.probes,
-                      m.dist};
+                      m.dist, m.order};
+        if (learned)
+        {
+            // each edge's group order first (one warp per edge), on the same stream
+            if (!m.order)
+            {
+                return set_error(VG_ERR_STATE, "learned-order check without an order buffer");
+            }
+            const long long owant = (static_cast<long long>(m.n) + kBlock / 32 - 1) / (kBlock / 32);
+            const int ogrid = static_cast<int>(std::min<long long>(owant, static_cast<long long>(sm_count()) * 16));
+            VG_CUDA(r->edge_order[which](p, ogrid, kBlock, 0, s), "edge order kernel launch");
+        }
         const auto launch = ext ? r->edges_ext[which]
                                 : learned ? r->edges_learned[which]
                                 : packed  ? r->edges_packed[which]
@@ -587,6 +598,8 @@ void vg_env_destroy(vg_env *env)
         cudaFree(env->d_counter);
     if (env->d_stage)
         cudaFree(env->d_stage);
+    if (env->d_order)
+        cudaFree(env->d_order);
     for (void *p : env->d_clouds)
         cudaFree(p);
     for (void *p : env->d_hf)
@@ -1040,7 +1053,17 @@ int vg_validate_motions_scored_device(
         return VG_OK;
     if (int rc = commit(env))
         return rc;
+    if (n * 16 > env->order_cap)
+    {
+        if (env->d_order)
+            cudaFree(env->d_order);
+        env->d_order = nullptr;
+        env->order_cap = 0;
+        VG_CUDA(cudaMalloc(&env->d_order, n * 16), "cudaMalloc(group orders)");
+        env->order_cap = n * 16;
+    }
     MotionLaunch m{r, env, a, b, n, resolution, scores, probes, out, blocks, env->d_counter};
+    m.order = env->d_order;
     int schedule = 1;
     tuned_for(env, r, &schedule, &m.blocks_per_sm);
     return launch_motions(m, static_cast<cudaStream_t>(stream));

@@ -34,6 +34,7 @@ struct vg_batch
     unsigned *counters = nullptr;  // one work counter per part (64 bytes apart)
     size_t counters_cap = 0;
     std::vector<float *> scores;   // per part with an MLP: [n][probes]
+    std::vector<uint8_t *> orders; // per part with an MLP: its edges' group orders, 16 bytes each
     cudaStream_t capture = nullptr;  // the graph is captured here (the caller's stream may be the legacy default stream, which cannot be captured)
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> events;
@@ -82,12 +83,18 @@ namespace
         }
         while (bt->scores.size() < bt->parts.size())
             bt->scores.push_back(nullptr);
+        while (bt->orders.size() < bt->parts.size())
+            bt->orders.push_back(nullptr);
         for (size_t i = 0; i < bt->parts.size(); ++i)
         {
             const auto &p = bt->parts[i];
             if (p.mlp && !bt->scores[i])
             {
                 VG_CUDA(cudaMalloc(&bt->scores[i], p.n * p.probes * sizeof(float)), "cudaMalloc(batch scores)");
+            }
+            if (p.mlp && !bt->orders[i])
+            {
+                VG_CUDA(cudaMalloc(&bt->orders[i], p.n * 16), "cudaMalloc(batch group orders)");
             }
         }
         if (!bt->capture)
@@ -125,6 +132,7 @@ namespace
             }
             MotionLaunch m{p.r, p.env, p.a, p.b, p.n, p.resolution, p.mlp ? bt->scores[i] : nullptr, p.probes,
                            p.out, p.blocks, bt->counters + 16 * i};
+            m.order = p.mlp ? bt->orders[i] : nullptr;
             tuned_for(p.env, p.r, &m.schedule, &m.blocks_per_sm);
             if (int rc = launch_motions(m, st))
                 return rc;
@@ -149,6 +157,9 @@ void vg_batch_destroy(vg_batch *b)
     drop_graph(b);
     if (b->counters)
         cudaFree(b->counters);
+    for (uint8_t *p : b->orders)
+        if (p)
+            cudaFree(p);
     for (float *p : b->scores)
         if (p)
             cudaFree(p);

@@ -43,7 +43,9 @@ namespace vg
         // next edge
         cudaError_t (*edges_packed[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_packed_fn[2];
-        // same-edge schedule in a learned block order (EdgesParams::scores)
+        // each edge's group order from its scores (before the learned-order check)
+        cudaError_t (*edge_order[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
+        // same-edge schedule in a learned block order (EdgesParams::order)
         cudaError_t (*edges_learned[2])(const EdgesParams &, int grid, int block, int smem, cudaStream_t);
         const void *edges_learned_fn[2];
         // extended forms (heightfields in the environment, or an attachment: fkcc_attach): states,
@@ -133,6 +135,9 @@ struct vg_env
     std::vector<vg::CaptHost> clouds;
     std::vector<void *> d_clouds;        // kCloudBuffers buffers per uploaded cloud
     std::vector<vg::CaptQuery> capt_q;   // per uploaded cloud (pointers into d_clouds)
+    // learned-order group orders (vg_validate_motions_scored_device), 16 bytes per edge
+    uint8_t *d_order = nullptr;
+    size_t order_cap = 0;
     // library-owned scratch: work counter, staging for host-pointer calls
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;
@@ -163,6 +168,7 @@ namespace vg
         int schedule = 1;      // 0: a segment per edge, 1: a warp per edge, 2: the same, register-rich build, 3: 2 packed
         int blocks_per_sm = 0;  // 0: as many as fit
         const float *dist = nullptr;  // validate_vector form: b holds vectors, dist their lengths
+        uint8_t *order = nullptr;     // with scores: scratch of n x 16 bytes for the group orders
     };
 
     int commit(vg_env *e);

@@ -270,6 +270,9 @@ namespace vg
         // validate_vector form (planning/validate.hh:23-63): b holds each edge's vector and dist
         // its length as the caller gives it (the block count follows it); null = validate_motion
         const float *dist = nullptr;
+        // learned order: per edge kOrderMax / (32 / W) group indices in checking order, written
+        // by edge_order_kernel from the scores
+        uint8_t *order = nullptr;
     };
 
     constexpr int kOrderMax = 64;  // blocks of an edge the learned order ranks; later ones follow in order
@@ -343,6 +346,12 @@ namespace vg
         __syncwarp();
     }
 
+    // The learned group order of every edge (one warp per edge) from its probe scores, for the
+    // same-edge check with the learned order: p.order[e][0 .. kOrderMax / (32 / W)).  Edges of
+    // one group (n <= 32 / W blocks) get the reference's order.
+    template <int D, int W>
+    __global__ void __launch_bounds__(128) edge_order_kernel(EdgesParams p);
+
     // |b - a| as the reference computes it on x86: squares summed lane-wise over the 8-wide
     // vectors that hold the configuration, then ((s0+s4)+(s2+s6)) + ((s1+s5)+(s3+s7)), then a
     // correctly rounded sqrt (vector/avx.hh:442-452, vector/interface.hh:402-410).
@@ -364,6 +373,46 @@ namespace vg
         const float a0 = __fadd_rn(s[4], s[0]), a1 = __fadd_rn(s[5], s[1]);
         const float a2 = __fadd_rn(s[6], s[2]), a3 = __fadd_rn(s[7], s[3]);
         return __fsqrt_rn(__fadd_rn(__fadd_rn(a0, a2), __fadd_rn(a1, a3)));
+    }
+
+    template <int D, int W>
+    __global__ void __launch_bounds__(128) edge_order_kernel(EdgesParams p)
+    {
+        constexpr int S = 32 / W;
+        constexpr int kGroups = kOrderMax / S;
+        __shared__ uint8_t s_order[4][kOrderMax];
+        const int lane = threadIdx.x & 31;
+        uint8_t *order = s_order[(threadIdx.x >> 5) & 3];
+        const long long warps = static_cast<long long>(gridDim.x) * (blockDim.x >> 5);
+        for (long long e = static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); e < p.n; e += warps)
+        {
+            // the block count exactly as the edge kernels compute it
+            float v[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                const float av = p.a[e * D + d];
+                v[d] = p.dist ? p.b[e * D + d] : __fsub_rn(p.b[e * D + d], av);
+            }
+            const float len = p.dist ? p.dist[e] : edge_length<D>(v);
+            const float t = __fmul_rn(__fdiv_rn(len, static_cast<float>(W)), static_cast<float>(p.resolution));
+            const float nf = ceilf(t);
+            const int n = static_cast<int>(nf > 1.0f ? nf : 1.0f);
+            if (lane < kGroups)
+            {
+                order[lane] = static_cast<uint8_t>(lane);
+            }
+            __syncwarp();
+            if (n > S)
+            {
+                learned_order<W>(p.scores + e * p.probes, p.probes, n, order);
+            }
+            if (lane < kGroups)
+            {
+                p.order[e * kGroups + lane] = order[lane];
+            }
+            __syncwarp();
+        }
     }
 
     template <typename Robot, int W, bool kExt = false>
@@ -494,7 +543,6 @@ namespace vg
         const float pct = __fdiv_rn(static_cast<float>(sl + 1), static_cast<float>(W));
         constexpr unsigned kSegBits = W == 32 ? kFull : ((1u << W) - 1u);
         constexpr unsigned kSegLeaders = W == 8 ? 0x01010101u : (W == 4 ? 0x11111111u : 1u);
-        __shared__ uint8_t s_order[kLearned ? 4 : 1][kOrderMax];
 
         for (;;)
         {
@@ -534,13 +582,11 @@ namespace vg
             int verdict = 1, checked = n;
             if constexpr (kLearned)
             {
-                uint8_t *order = s_order[threadIdx.x >> 5];
-                const bool learned = n > S;
-                if (learned)
-                {
-                    learned_order<W>(p.scores + static_cast<long long>(e) * p.probes, p.probes, n, order);
-                }
+                // the group order edge_order_kernel wrote for this edge (edges of one group keep
+                // the reference's order)
                 constexpr int kGroups = kOrderMax / S;
+                const uint8_t *order = p.order + static_cast<long long>(e) * kGroups;
+                const bool learned = n > S;
                 int done = 0;  // blocks checked in earlier iterations
                 for (int i0 = 0; i0 < n; i0 += S)
                 {
@@ -551,10 +597,15 @@ namespace vg
                     {
                         if (want < cur)
                         {
+                            // back to block 0: the edge's vector is re-read rather than kept in
+                            // registers through the check (same values, same rounding)
 #pragma unroll
                             for (int d = 0; d < D; ++d)
                             {
-                                q[d] = __fmaf_rn(v[d], pct, p.a[static_cast<long long>(e) * D + d]);
+                                const float av = p.a[static_cast<long long>(e) * D + d];
+                                const float vd = p.dist ? p.b[static_cast<long long>(e) * D + d]
+                                                        : __fsub_rn(p.b[static_cast<long long>(e) * D + d], av);
+                                q[d] = __fmaf_rn(vd, pct, av);
                             }
                             cur = 0;
                         }

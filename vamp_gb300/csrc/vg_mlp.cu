@@ -737,12 +737,19 @@ namespace vg
                + 3u * kHidden * 4;                           // b1, b2, w3
     }
 
+    // Threads of the fused inference kernel: 16 warps.  Warp w reads TMEM lanes 32 (w % 4) ..
+    // 32 (w % 4) + 31 (the rows of its lane quarter, as tcgen05.ld allows) and columns
+    // 64 (w / 4) .. 64 (w / 4) + 63 of each 256-column accumulator, so four warps share each
+    // quarter's epilogue work and every scheduler has four warps to switch between.
+    constexpr int kInferThreads = 512;
+
     template <int KIN>
-    __global__ void __launch_bounds__(128, 1) mlp_infer_kernel(const InferParams p)
+    __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const InferParams p)
     {
         extern __shared__ __align__(1024) unsigned char infer_smem[];
         __shared__ uint64_t bar;
         __shared__ uint32_t tmem_slot;
+        __shared__ float zpart[4][128];  // partial dot products per column slice and row
         unsigned char *sw1 = infer_smem;
         unsigned char *sw2 = sw1 + kHidden * KIN * 2;
         unsigned char *sx = sw2 + kHidden * kHidden * 2;
@@ -752,6 +759,9 @@ namespace vg
         float *sw3 = sb2 + kHidden;
         const int tid = threadIdx.x;
         const int warp = tid >> 5;
+        const int quarter = warp & 3;               // TMEM lane quarter
+        const int slice = warp >> 2;                // 64-column slice
+        const int row = 32 * quarter + (tid & 31);  // tile row of this thread in the epilogues
         __shared__ int skip;
 
         if (tid == 0)
@@ -764,19 +774,19 @@ namespace vg
         if (tid == 0)
             tc::mbar_init(&bar, 1);
         // weights into core-matrix layout, 16-byte units
-        for (int u = tid; u < kHidden * (KIN / 8); u += 128)
+        for (int u = tid; u < kHidden * (KIN / 8); u += kInferThreads)
         {
             const int r = u / (KIN / 8), g = u % (KIN / 8);
             *reinterpret_cast<uint4 *>(sw1 + tc::tile_offset(r, 8 * g, KIN)) =
                 *reinterpret_cast<const uint4 *>(p.w1 + static_cast<size_t>(r) * KIN + 8 * g);
         }
-        for (int u = tid; u < kHidden * (kHidden / 8); u += 128)
+        for (int u = tid; u < kHidden * (kHidden / 8); u += kInferThreads)
         {
             const int r = u / (kHidden / 8), g = u % (kHidden / 8);
             *reinterpret_cast<uint4 *>(sw2 + tc::tile_offset(r, 8 * g, kHidden)) =
                 *reinterpret_cast<const uint4 *>(p.w2 + static_cast<size_t>(r) * kHidden + 8 * g);
         }
-        for (int j = tid; j < kHidden; j += 128)
+        for (int j = tid; j < kHidden; j += kInferThreads)
         {
             sb1[j] = p.b1[j];
             sb2[j] = p.b2[j];
@@ -787,7 +797,8 @@ namespace vg
         __syncthreads();
         tc::fence_after_sync();
         const uint32_t tmem = tmem_slot;
-        const uint32_t lane_base = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        const uint32_t lane_base = tmem + (static_cast<uint32_t>(quarter * 32) << 16);
+        const int c_lo = 64 * slice;  // this warp's first accumulator column
         const uint32_t idesc = tc::idesc_bf16_f32(128, kHidden);
         uint32_t phase = 0;
         bool ok = true;
@@ -795,30 +806,38 @@ namespace vg
 
         for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x)
         {
-            const long long g = tile * 128 + tid;
-            // ---- features of this thread's row
+            // ---- features: thread (frow, unit) writes the 8 features of one 16-byte unit of a row
             {
-                __align__(16) __nv_bfloat16 f[KIN];
-#pragma unroll
-                for (int c = 0; c < KIN; ++c)
-                    f[c] = __float2bfloat16_rn(0.0f);
-                if (g < p.rows)
+                const int frow = tid & 127;
+                const int unit = tid >> 7;  // 0..3; KIN / 8 units per row
+                if (unit < KIN / 8)
                 {
-                    const long long e = g / p.probes;
-                    const int pr = static_cast<int>(g - e * p.probes);
-                    const float t = (static_cast<float>(pr) + 0.5f) / static_cast<float>(p.probes);
-                    for (int d = 0; d < p.dim; ++d)
-                    {
-                        float q = p.a[e * p.dim + d];
-                        if (p.b)
-                            q = fmaf(p.b[e * p.dim + d] - q, t, q);
-                        f[2 * d] = __float2bfloat16_rn(sinf(q));
-                        f[2 * d + 1] = __float2bfloat16_rn(cosf(q));
-                    }
-                }
+                    const long long g = tile * 128 + frow;
+                    __align__(16) __nv_bfloat16 f[8];
 #pragma unroll
-                for (int c = 0; c < KIN; c += 8)
-                    *reinterpret_cast<uint4 *>(sx + tc::tile_offset(tid, c, KIN)) = *reinterpret_cast<const uint4 *>(&f[c]);
+                    for (int c = 0; c < 8; ++c)
+                        f[c] = __float2bfloat16_rn(0.0f);
+                    if (g < p.rows)
+                    {
+                        const long long e = g / p.probes;
+                        const int pr = static_cast<int>(g - e * p.probes);
+                        const float t = (static_cast<float>(pr) + 0.5f) / static_cast<float>(p.probes);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const int d = 4 * unit + k;  // features 2d, 2d + 1
+                            if (d < p.dim)
+                            {
+                                float q = p.a[e * p.dim + d];
+                                if (p.b)
+                                    q = fmaf(p.b[e * p.dim + d] - q, t, q);
+                                f[2 * k] = __float2bfloat16_rn(sinf(q));
+                                f[2 * k + 1] = __float2bfloat16_rn(cosf(q));
+                            }
+                        }
+                    }
+                    *reinterpret_cast<uint4 *>(sx + tc::tile_offset(frow, 8 * unit, KIN)) = *reinterpret_cast<const uint4 *>(f);
+                }
             }
             tc::fence_smem_to_async();
             tc::fence_before_sync();
@@ -841,8 +860,9 @@ namespace vg
                 break;
             }
             tc::fence_after_sync();
-            // ---- H1 = bf16(relu(D1 + b1)) into shared memory, row tid
-            for (int c0 = 0; c0 < kHidden; c0 += 32)
+            // ---- H1 = bf16(relu(D1 + b1)) into shared memory: this warp's rows and column slice
+#pragma unroll
+            for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
             {
                 float v[32];
                 tc::tmem_load32(lane_base + static_cast<uint32_t>(c0), v);
@@ -853,7 +873,7 @@ namespace vg
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
                         h[k] = __float2bfloat16_rn(fmaxf(__fadd_rn(v[j + k], sb1[c0 + j + k]), 0.0f));
-                    *reinterpret_cast<uint4 *>(sh + tc::tile_offset(tid, c0 + j, kHidden)) = *reinterpret_cast<const uint4 *>(h);
+                    *reinterpret_cast<uint4 *>(sh + tc::tile_offset(row, c0 + j, kHidden)) = *reinterpret_cast<const uint4 *>(h);
                 }
             }
             tc::fence_smem_to_async();
@@ -877,9 +897,11 @@ namespace vg
                 break;
             }
             tc::fence_after_sync();
-            // ---- z = bf16(relu(D2 + b2)) . w3 + b3
+            // ---- z = bf16(relu(D2 + b2)) . w3 + b3: partial sums over this warp's 64 columns,
+            // added slice by slice in column order
             float z = 0.0f;
-            for (int c0 = 0; c0 < kHidden; c0 += 32)
+#pragma unroll
+            for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
             {
                 float v[32];
                 tc::tmem_load32(lane_base + static_cast<uint32_t>(kHidden + c0), v);
@@ -890,10 +912,17 @@ namespace vg
                     z = fmaf(h, sw3[c0 + j], z);
                 }
             }
-            z += b3;
-            if (g < p.rows)
-                p.out[g] = p.probability ? 1.0f / (1.0f + expf(-z)) : z;
+            zpart[slice][row] = z;
             tc::fence_before_sync();
+            __syncthreads();
+            if (slice == 0)
+            {
+                const long long g = tile * 128 + row;
+                const float zz = ((zpart[0][row] + zpart[1][row]) + (zpart[2][row] + zpart[3][row])) + b3;
+                if (g < p.rows)
+                    p.out[g] = p.probability ? 1.0f / (1.0f + expf(-zz)) : zz;
+            }
+            // zpart is rewritten only after the next tile's two MMA waits (each behind a barrier)
         }
         if (!ok && tid == 0)
         {
@@ -914,6 +943,8 @@ namespace vg
     {
         if (rows == 0)
             return VG_OK;
+        if (m->kin > 32)
+            return set_error(VG_ERR_LIMIT, "MLP inference: at most 16 joints (32 sin/cos features)");
         InferParams ip{a, b, probes, rows, m->dim, m->w1b, m->w2b, m->B1(), m->B2(), m->W3(), m->B3(), out, probability, m->err};
         ip.wait_limit = m->wait_limit;
         int dev = 0, sms = 0;
@@ -928,7 +959,7 @@ namespace vg
             e = cudaFuncSetAttribute(mlp_infer_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
             if (e == cudaSuccess)
             {
-                mlp_infer_kernel<16><<<grid, 128, smem, s>>>(ip);
+                mlp_infer_kernel<16><<<grid, kInferThreads, smem, s>>>(ip);
                 e = cudaGetLastError();
             }
         }
@@ -938,7 +969,7 @@ namespace vg
             e = cudaFuncSetAttribute(mlp_infer_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
             if (e == cudaSuccess)
             {
-                mlp_infer_kernel<32><<<grid, 128, smem, s>>>(ip);
+                mlp_infer_kernel<32><<<grid, kInferThreads, smem, s>>>(ip);
                 e = cudaGetLastError();
             }
         }

@@ -45,6 +45,13 @@ namespace vg
         return cudaGetLastError();
     }
 
+    template <typename R, int W>
+    cudaError_t launch_edge_order(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
+    {
+        edge_order_kernel<R::kDim, W><<<grid, block, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+
     template <typename R, int W, int kMinBlocks, bool kLoopedEnv>
     cudaError_t launch_edges_packed(const EdgesParams &p, int grid, int block, int smem, cudaStream_t s)
     {
@@ -116,10 +123,15 @@ namespace vg
         o.edges_packed[1] = &launch_edges_packed<R, 4, VG_MIN_BLOCKS_WIDE, true>;
         o.edges_packed_fn[0] = reinterpret_cast<const void *>(&edges_packed_kernel<R, 8, VG_MIN_BLOCKS_WIDE, true>);
         o.edges_packed_fn[1] = reinterpret_cast<const void *>(&edges_packed_kernel<R, 4, VG_MIN_BLOCKS_WIDE, true>);
-        o.edges_learned[0] = &launch_edges_grouped<R, 8, true>;
-        o.edges_learned[1] = &launch_edges_grouped<R, 4, true>;
-        o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true>);
-        o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true>);
+        // the learned order in the form of the fastest plain schedule for the Panda, UR5 and Fetch
+        // (register-rich build, looped environment section); the group order comes precomputed
+        // (edge_order_kernel), which keeps it within the registers of 4 resident blocks
+        o.edges_learned[0] = &launch_edges_grouped<R, 8, true, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_learned[1] = &launch_edges_grouped<R, 4, true, VG_MIN_BLOCKS_WIDE, true>;
+        o.edges_learned_fn[0] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 8, true, VG_MIN_BLOCKS_WIDE, true>);
+        o.edges_learned_fn[1] = reinterpret_cast<const void *>(&edges_grouped_kernel<R, 4, true, VG_MIN_BLOCKS_WIDE, true>);
+        o.edge_order[0] = &launch_edge_order<R, 8>;
+        o.edge_order[1] = &launch_edge_order<R, 4>;
         // extended checks (heightfields, fkcc_attach): the segment-per-edge and states kernels
         o.states_ext = &launch_states<R, true>;
         o.states_ext_fn = reinterpret_cast<const void *>(&states_kernel<R, true>);
