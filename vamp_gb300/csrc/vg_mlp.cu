@@ -743,11 +743,17 @@ namespace vg
     // quarter's epilogue work and every scheduler has four warps to switch between.
     constexpr int kInferThreads = 512;
 
+    // Per 128-row tile: layer 1 (X W1^T into TMEM columns 0-255), bias + ReLU to BF16 in shared
+    // memory (H1), layer 2 (H1 W2^T into columns 256-511), bias + ReLU + dot with w3.  Tiles are
+    // pipelined: the next tile's features are computed while this tile's layer 2 runs on the
+    // tensor cores, and the next tile's layer 1 runs while this tile's layer-2 epilogue reads its
+    // columns.  One mbarrier per layer; every wait is bounded, and a kernel that gives up waits
+    // (with the default limit) for the MMAs it issued before it frees the tensor memory.
     template <int KIN>
     __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const InferParams p)
     {
         extern __shared__ __align__(1024) unsigned char infer_smem[];
-        __shared__ uint64_t bar;
+        __shared__ uint64_t bar1, bar2;
         __shared__ uint32_t tmem_slot;
         __shared__ float zpart[4][128];  // partial dot products per column slice and row
         unsigned char *sw1 = infer_smem;
@@ -772,7 +778,10 @@ namespace vg
         if (warp == 0)
             tc::tmem_alloc(&tmem_slot, 512);
         if (tid == 0)
-            tc::mbar_init(&bar, 1);
+        {
+            tc::mbar_init(&bar1, 1);
+            tc::mbar_init(&bar2, 1);
+        }
         // weights into core-matrix layout, 16-byte units
         for (int u = tid; u < kHidden * (KIN / 8); u += kInferThreads)
         {
@@ -800,48 +809,44 @@ namespace vg
         const uint32_t lane_base = tmem + (static_cast<uint32_t>(quarter * 32) << 16);
         const int c_lo = 64 * slice;  // this warp's first accumulator column
         const uint32_t idesc = tc::idesc_bf16_f32(128, kHidden);
-        uint32_t phase = 0;
-        bool ok = true;
+        uint32_t ph1 = 0, ph2 = 0;     // phases the next waits on bar1 / bar2 expect
+        bool pend1 = false, pend2 = false;  // an MMA group committed to bar1 / bar2 and not yet waited for
         const long long tiles = (p.rows + 127) / 128;
 
-        for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x)
-        {
-            // ---- features: thread (frow, unit) writes the 8 features of one 16-byte unit of a row
+        // features of a tile: thread (frow, unit) writes the 8 features of one 16-byte unit
+        auto features = [&](long long tile) {
+            const int frow = tid & 127;
+            const int unit = tid >> 7;  // 0..3; KIN / 8 units per row
+            if (unit < KIN / 8)
             {
-                const int frow = tid & 127;
-                const int unit = tid >> 7;  // 0..3; KIN / 8 units per row
-                if (unit < KIN / 8)
+                const long long g = tile * 128 + frow;
+                __align__(16) __nv_bfloat16 f[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    f[c] = __float2bfloat16_rn(0.0f);
+                if (g < p.rows)
                 {
-                    const long long g = tile * 128 + frow;
-                    __align__(16) __nv_bfloat16 f[8];
+                    const long long e = g / p.probes;
+                    const int pr = static_cast<int>(g - e * p.probes);
+                    const float t = (static_cast<float>(pr) + 0.5f) / static_cast<float>(p.probes);
 #pragma unroll
-                    for (int c = 0; c < 8; ++c)
-                        f[c] = __float2bfloat16_rn(0.0f);
-                    if (g < p.rows)
+                    for (int k = 0; k < 4; ++k)
                     {
-                        const long long e = g / p.probes;
-                        const int pr = static_cast<int>(g - e * p.probes);
-                        const float t = (static_cast<float>(pr) + 0.5f) / static_cast<float>(p.probes);
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
+                        const int d = 4 * unit + k;  // features 2d, 2d + 1
+                        if (d < p.dim)
                         {
-                            const int d = 4 * unit + k;  // features 2d, 2d + 1
-                            if (d < p.dim)
-                            {
-                                float q = p.a[e * p.dim + d];
-                                if (p.b)
-                                    q = fmaf(p.b[e * p.dim + d] - q, t, q);
-                                f[2 * k] = __float2bfloat16_rn(sinf(q));
-                                f[2 * k + 1] = __float2bfloat16_rn(cosf(q));
-                            }
+                            float q = p.a[e * p.dim + d];
+                            if (p.b)
+                                q = fmaf(p.b[e * p.dim + d] - q, t, q);
+                            f[2 * k] = __float2bfloat16_rn(sinf(q));
+                            f[2 * k + 1] = __float2bfloat16_rn(cosf(q));
                         }
                     }
-                    *reinterpret_cast<uint4 *>(sx + tc::tile_offset(frow, 8 * unit, KIN)) = *reinterpret_cast<const uint4 *>(f);
                 }
+                *reinterpret_cast<uint4 *>(sx + tc::tile_offset(frow, 8 * unit, KIN)) = *reinterpret_cast<const uint4 *>(f);
             }
-            tc::fence_smem_to_async();
-            tc::fence_before_sync();
-            __syncthreads();
+        };
+        auto issue_layer1 = [&]() {
             if (tid == 0)
             {
                 tc::fence_after_sync();
@@ -850,35 +855,11 @@ namespace vg
                 for (int kk = 0; kk < KIN / 16; ++kk)
                     tc::mma_bf16(tmem, tc::smem_desc(x0 + kk * 256, 128, (KIN / 8) * 128),
                                  tc::smem_desc(w0 + kk * 256, 128, (KIN / 8) * 128), idesc, kk > 0);
-                tc::mma_commit(&bar);
+                tc::mma_commit(&bar1);
             }
-            ok = tc::mbar_wait(&bar, phase, p.wait_limit);
-            phase ^= 1u;
-            if (!__syncthreads_and(ok))
-            {
-                ok = false;
-                break;
-            }
-            tc::fence_after_sync();
-            // ---- H1 = bf16(relu(D1 + b1)) into shared memory: this warp's rows and column slice
-#pragma unroll
-            for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
-            {
-                float v[32];
-                tc::tmem_load32(lane_base + static_cast<uint32_t>(c0), v);
-#pragma unroll
-                for (int j = 0; j < 32; j += 8)
-                {
-                    __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-                    for (int k = 0; k < 8; ++k)
-                        h[k] = __float2bfloat16_rn(fmaxf(__fadd_rn(v[j + k], sb1[c0 + j + k]), 0.0f));
-                    *reinterpret_cast<uint4 *>(sh + tc::tile_offset(row, c0 + j, kHidden)) = *reinterpret_cast<const uint4 *>(h);
-                }
-            }
-            tc::fence_smem_to_async();
-            tc::fence_before_sync();
-            __syncthreads();
+            pend1 = true;
+        };
+        auto issue_layer2 = [&]() {
             if (tid == 0)
             {
                 tc::fence_after_sync();
@@ -887,18 +868,48 @@ namespace vg
                 for (int kk = 0; kk < kHidden / 16; ++kk)
                     tc::mma_bf16(tmem + kHidden, tc::smem_desc(h0 + kk * 256, 128, (kHidden / 8) * 128),
                                  tc::smem_desc(w0 + kk * 256, 128, (kHidden / 8) * 128), idesc, kk > 0);
-                tc::mma_commit(&bar);
+                tc::mma_commit(&bar2);
             }
-            ok = tc::mbar_wait(&bar, phase, p.wait_limit);
-            phase ^= 1u;
-            if (!__syncthreads_and(ok))
+            pend2 = true;
+        };
+        // bounded wait for the group committed to bar; every thread takes the same decision
+        auto wait_for = [&](uint64_t *bar, uint32_t &ph, bool &pend) {
+            bool ok = tc::mbar_wait(bar, ph, p.wait_limit);
+            ok = __syncthreads_and(ok) != 0;
+            if (ok)
             {
-                ok = false;
-                break;
+                ph ^= 1u;
+                pend = false;
+                tc::fence_after_sync();
             }
-            tc::fence_after_sync();
-            // ---- z = bf16(relu(D2 + b2)) . w3 + b3: partial sums over this warp's 64 columns,
-            // added slice by slice in column order
+            return ok;
+        };
+        // H1 = bf16(relu(D1 + b1)) into shared memory: this warp's rows and column slice
+        auto epilogue1 = [&]() {
+#pragma unroll
+            for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
+            {
+                float v[32];
+                tc::tmem_load32(lane_base + static_cast<uint32_t>(c0), v);
+#pragma unroll
+                for (int j = 0; j < 32; j += 8)
+                {
+                    // two values per conversion instruction, each rounded to nearest as before
+                    __align__(16) __nv_bfloat162 h[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        h[k] = __floats2bfloat162_rn(fmaxf(__fadd_rn(v[j + 2 * k], sb1[c0 + j + 2 * k]), 0.0f),
+                                                     fmaxf(__fadd_rn(v[j + 2 * k + 1], sb1[c0 + j + 2 * k + 1]), 0.0f));
+                    *reinterpret_cast<uint4 *>(sh + tc::tile_offset(row, c0 + j, kHidden)) = *reinterpret_cast<const uint4 *>(h);
+                }
+            }
+            tc::fence_smem_to_async();
+            tc::fence_before_sync();
+            __syncthreads();
+        };
+        // z = bf16(relu(D2 + b2)) . w3 + b3: partial sums over this warp's 64 columns, added
+        // slice by slice in column order
+        auto epilogue2 = [&](long long tile) {
             float z = 0.0f;
 #pragma unroll
             for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
@@ -906,10 +917,12 @@ namespace vg
                 float v[32];
                 tc::tmem_load32(lane_base + static_cast<uint32_t>(kHidden + c0), v);
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
+                for (int j = 0; j < 32; j += 2)
                 {
-                    const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(__fadd_rn(v[j], sb2[c0 + j]), 0.0f)));
-                    z = fmaf(h, sw3[c0 + j], z);
+                    const float2 h = __bfloat1622float2(__floats2bfloat162_rn(fmaxf(__fadd_rn(v[j], sb2[c0 + j]), 0.0f),
+                                                                              fmaxf(__fadd_rn(v[j + 1], sb2[c0 + j + 1]), 0.0f)));
+                    z = fmaf(h.x, sw3[c0 + j], z);
+                    z = fmaf(h.y, sw3[c0 + j + 1], z);
                 }
             }
             zpart[slice][row] = z;
@@ -922,12 +935,58 @@ namespace vg
                 if (g < p.rows)
                     p.out[g] = p.probability ? 1.0f / (1.0f + expf(-zz)) : zz;
             }
-            // zpart is rewritten only after the next tile's two MMA waits (each behind a barrier)
+            // zpart is written again only after two more block-wide barriers
+        };
+
+        bool ok = true;
+        long long tile = blockIdx.x;
+        if (tile < tiles)
+        {
+            // prologue: layer 1 of the first tile, then its layer 2 in flight
+            features(tile);
+            tc::fence_smem_to_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            issue_layer1();
+            ok = wait_for(&bar1, ph1, pend1);
+            if (ok)
+            {
+                epilogue1();
+                issue_layer2();
+            }
+            while (ok)
+            {
+                const long long next = tile + gridDim.x;
+                const bool has_next = next < tiles;
+                if (has_next)
+                    features(next);  // while this tile's layer 2 runs
+                tc::fence_smem_to_async();
+                tc::fence_before_sync();
+                __syncthreads();
+                ok = wait_for(&bar2, ph2, pend2);
+                if (!ok)
+                    break;
+                if (has_next)
+                    issue_layer1();  // runs while this tile's layer-2 epilogue reads columns 256-511
+                epilogue2(tile);
+                if (!has_next)
+                    break;
+                ok = wait_for(&bar1, ph1, pend1);
+                if (!ok)
+                    break;
+                epilogue1();
+                issue_layer2();
+                tile = next;
+            }
         }
         if (!ok && tid == 0)
         {
             atomicExch(p.err, 1);
-            tc::mbar_wait(&bar, phase ^ 1u, kWaitLimit);
+            // let the MMAs still in flight finish before the accumulator is released
+            if (pend1)
+                tc::mbar_wait(&bar1, ph1, kWaitLimit);
+            if (pend2)
+                tc::mbar_wait(&bar2, ph2, kWaitLimit);
         }
         tc::fence_before_sync();
         __syncthreads();
