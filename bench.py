@@ -280,6 +280,8 @@ def cpu_baseline(scene, a, b, budget_s: float = 10.0):
            "sample": f"{done} edges of the workload ({n} per pass), {threads} host threads, {elapsed:.1f} s"}
     if kind == "port":
         out["reference_x86"] = REFERENCE_X86
+    else:
+        out["build"] = "x86-64 AVX2, 8 lanes" if os.uname().machine == "x86_64" else "aarch64 NEON, 4 lanes"
     return out
 
 

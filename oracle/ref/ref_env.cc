@@ -293,21 +293,43 @@ void vgref_vec_sincos8(const float *in, float *s, float *c)
     std::memcpy(c, rc.data(), 32);
 }
 
+}  // extern "C"
+
+namespace
+{
+    // The 8-lane query where the build's environment holds 8-lane vectors (the AVX2 build); -1
+    // in a 4-lane (NEON) build.
+    template <std::size_t L>
+    int sphere_env_lanes(RefEnv *e, const float *xs, const float *ys, const float *zs, const float *rs)
+    {
+        if constexpr (L == 8)
+        {
+            std::array<float, 8> ax, ay, az, ar;
+            std::memcpy(ax.data(), xs, 32);
+            std::memcpy(ay.data(), ys, 32);
+            std::memcpy(az.data(), zs, 32);
+            std::memcpy(ar.data(), rs, 32);
+            return sphere_environment_in_collision(
+                       *e->vec, FloatVector<8>(ax), FloatVector<8>(ay), FloatVector<8>(az), FloatVector<8>(ar)) ?
+                       1 :
+                       0;
+        }
+        else
+        {
+            return -1;
+        }
+    }
+}  // namespace
+
+extern "C" {
+
 // One sphere query (8 lanes) against the environment: sphere_environment_in_collision
-// (collision/validity.hh:47-150).  Returns 1 on collision.
+// (collision/validity.hh:47-150).  Returns 1 on collision (-1 in a 4-lane build).
 int vgref_sphere_env8(void *h, const float *xs, const float *ys, const float *zs, const float *rs)
 {
     auto *e = static_cast<RefEnv *>(h);
     e->finalize();
-    std::array<float, 8> ax, ay, az, ar;
-    std::memcpy(ax.data(), xs, 32);
-    std::memcpy(ay.data(), ys, 32);
-    std::memcpy(az.data(), zs, 32);
-    std::memcpy(ar.data(), rs, 32);
-    return sphere_environment_in_collision(
-               *e->vec, FloatVector<8>(ax), FloatVector<8>(ay), FloatVector<8>(az), FloatVector<8>(ar)) ?
-               1 :
-               0;
+    return sphere_env_lanes<FloatVectorWidth>(e, xs, ys, zs, rs);
 }
 
 int vgref_lanes(void)
