@@ -702,8 +702,8 @@ int vg_mlp_train_device(vg_mlp *m, const float *q_dev, const uint8_t *valid_dev,
 
 // =============================================================================================
 // Fused inference: one persistent CTA per SM keeps W1 and W2 (BF16, core-matrix layout) in
-// shared memory and, per 128-row tile, computes features -> L1 (one tcgen05 MMA group into TMEM
-// columns 0..255) -> bias+ReLU -> BF16 H1 in shared memory -> L2 (TMEM columns 256..511) ->
+// shared memory and, per 128-row tile, computes features -> L1 (one tcgen05 MMA group into half
+// of the TMEM columns) -> bias+ReLU -> BF16 H1 in shared memory -> L2 (the same half) ->
 // bias+ReLU -> BF16 H2 -> dot with w3 in registers.  Nothing but the scores leaves the SM.
 //
 // Row g scores a state: with b == nullptr, configuration a[g]; otherwise probe p = g % P of edge
@@ -711,6 +711,20 @@ int vg_mlp_train_device(vg_mlp *m, const float *q_dev, const uint8_t *valid_dev,
 
 namespace vg
 {
+    // bf16x2 {lo: relu(v.x), hi: relu(v.y)}, each rounded to nearest
+    __device__ __forceinline__ uint32_t relu_bf16x2(float2 v)
+    {
+        uint32_t h;
+        asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(v.y), "f"(v.x));
+        return h;
+    }
+
+    // the two BF16 halves of h as floats {lo, hi}
+    __device__ __forceinline__ float2 bf16x2_to_float2(uint32_t h)
+    {
+        return make_float2(__uint_as_float(h << 16), __uint_as_float(h & 0xffff0000u));
+    }
+
     struct InferParams
     {
         const float *a;
@@ -743,12 +757,13 @@ namespace vg
     // quarter's epilogue work and every scheduler has four warps to switch between.
     constexpr int kInferThreads = 512;
 
-    // Per 128-row tile: layer 1 (X W1^T into TMEM columns 0-255), bias + ReLU to BF16 in shared
-    // memory (H1), layer 2 (H1 W2^T into columns 256-511), bias + ReLU + dot with w3.  Tiles are
-    // pipelined: the next tile's features are computed while this tile's layer 2 runs on the
-    // tensor cores, and the next tile's layer 1 runs while this tile's layer-2 epilogue reads its
-    // columns.  One mbarrier per layer; every wait is bounded, and a kernel that gives up waits
-    // (with the default limit) for the MMAs it issued before it frees the tensor memory.
+    // Per 128-row tile: layer 1 (X W1^T into one half of the 512 TMEM columns), bias + ReLU to
+    // BF16 in shared memory (H1), layer 2 (H1 W2^T into the same half), bias + ReLU + dot with
+    // w3.  Tiles alternate halves and are pipelined: the next tile's features are computed while
+    // this tile's layer 2 runs, and the next tile's layer 2 runs while this tile's layer-2
+    // epilogue reads the other half.  One mbarrier per layer; every wait is bounded, and a kernel
+    // that gives up waits (with the default limit) for the MMAs it issued before it frees the
+    // tensor memory.
     template <int KIN>
     __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const InferParams p)
     {
@@ -813,60 +828,87 @@ namespace vg
         bool pend1 = false, pend2 = false;  // an MMA group committed to bar1 / bar2 and not yet waited for
         const long long tiles = (p.rows + 127) / 128;
 
-        // features of a tile: thread (frow, unit) writes the 8 features of one 16-byte unit
-        auto features = [&](long long tile) {
-            const int frow = tid & 127;
-            const int unit = tid >> 7;  // 0..3; KIN / 8 units per row
-            if (unit < KIN / 8)
+        // features of a tile: item i (row i % 128, joint d = i / 128) writes sin and cos of joint
+        // d of its row's state (zeros past the robot's joints); every thread takes KIN / 8 items,
+        // all of one row, so that all 16 warps share the sines and cosines.  A tile's first row
+        // g0 = e0 P + r0 is carried from tile to tile (tiles advance by a fixed number of rows),
+        // which leaves one 32-bit division per thread and tile, and each call loads the joint
+        // values of the CTA's following tile, so that their latency passes under a whole tile.
+        constexpr int kItems = KIN / 8;
+        const int frow = tid & 127;
+        const long long step_rows = static_cast<long long>(gridDim.x) * 128;
+        const long long step_e = step_rows / p.probes;
+        const int step_r = static_cast<int>(step_rows - step_e * p.probes);
+        long long ftile = blockIdx.x;  // the tile the loaded values belong to
+        long long e0 = ftile * 128 / p.probes;
+        int r0 = static_cast<int>(ftile * 128 - e0 * p.probes);
+        float in_a[kItems], in_v[kItems], in_t = 0.0f;
+        bool in_row = false;
+        auto load_inputs = [&]() {
+            const int loc = r0 + frow;
+            const long long e = e0 + loc / p.probes;
+            in_t = (static_cast<float>(loc % p.probes) + 0.5f) / static_cast<float>(p.probes);
+            in_row = ftile * 128 + frow < p.rows;
+#pragma unroll
+            for (int k = 0; k < kItems; ++k)
             {
-                const long long g = tile * 128 + frow;
-                __align__(16) __nv_bfloat16 f[8];
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    f[c] = __float2bfloat16_rn(0.0f);
-                if (g < p.rows)
+                const int d = (tid >> 7) + 4 * k;
+                in_a[k] = 0.0f;
+                in_v[k] = 0.0f;
+                if (in_row && d < p.dim)
                 {
-                    const long long e = g / p.probes;
-                    const int pr = static_cast<int>(g - e * p.probes);
-                    const float t = (static_cast<float>(pr) + 0.5f) / static_cast<float>(p.probes);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                    {
-                        const int d = 4 * unit + k;  // features 2d, 2d + 1
-                        if (d < p.dim)
-                        {
-                            float q = p.a[e * p.dim + d];
-                            if (p.b)
-                                q = fmaf(p.b[e * p.dim + d] - q, t, q);
-                            f[2 * k] = __float2bfloat16_rn(sinf(q));
-                            f[2 * k + 1] = __float2bfloat16_rn(cosf(q));
-                        }
-                    }
+                    in_a[k] = p.a[e * p.dim + d];
+                    if (p.b)
+                        in_v[k] = p.b[e * p.dim + d] - in_a[k];
                 }
-                *reinterpret_cast<uint4 *>(sx + tc::tile_offset(frow, 8 * unit, KIN)) = *reinterpret_cast<const uint4 *>(f);
             }
         };
-        auto issue_layer1 = [&]() {
+        auto features = [&]() {
+#pragma unroll
+            for (int k = 0; k < kItems; ++k)
+            {
+                const int d = (tid >> 7) + 4 * k;
+                __nv_bfloat162 f = __floats2bfloat162_rn(0.0f, 0.0f);
+                if (in_row && d < p.dim)
+                {
+                    const float q = p.b ? fmaf(in_v[k], in_t, in_a[k]) : in_a[k];
+                    f = __floats2bfloat162_rn(sinf(q), cosf(q));
+                }
+                *reinterpret_cast<__nv_bfloat162 *>(sx + tc::tile_offset(frow, 2 * d, KIN)) = f;
+            }
+            // the CTA's next tile
+            ftile += gridDim.x;
+            e0 += step_e;
+            r0 += step_r;
+            if (r0 >= p.probes)
+            {
+                r0 -= p.probes;
+                ++e0;
+            }
+            if (ftile < tiles)
+                load_inputs();
+        };
+        auto issue_layer1 = [&](uint32_t acc) {
             if (tid == 0)
             {
                 tc::fence_after_sync();
                 const uint32_t x0 = tc::smem_u32(sx), w0 = tc::smem_u32(sw1);
 #pragma unroll
                 for (int kk = 0; kk < KIN / 16; ++kk)
-                    tc::mma_bf16(tmem, tc::smem_desc(x0 + kk * 256, 128, (KIN / 8) * 128),
+                    tc::mma_bf16(tmem + acc, tc::smem_desc(x0 + kk * 256, 128, (KIN / 8) * 128),
                                  tc::smem_desc(w0 + kk * 256, 128, (KIN / 8) * 128), idesc, kk > 0);
                 tc::mma_commit(&bar1);
             }
             pend1 = true;
         };
-        auto issue_layer2 = [&]() {
+        auto issue_layer2 = [&](uint32_t acc) {
             if (tid == 0)
             {
                 tc::fence_after_sync();
                 const uint32_t h0 = tc::smem_u32(sh), w0 = tc::smem_u32(sw2);
 #pragma unroll 4
                 for (int kk = 0; kk < kHidden / 16; ++kk)
-                    tc::mma_bf16(tmem + kHidden, tc::smem_desc(h0 + kk * 256, 128, (kHidden / 8) * 128),
+                    tc::mma_bf16(tmem + acc, tc::smem_desc(h0 + kk * 256, 128, (kHidden / 8) * 128),
                                  tc::smem_desc(w0 + kk * 256, 128, (kHidden / 8) * 128), idesc, kk > 0);
                 tc::mma_commit(&bar2);
             }
@@ -884,22 +926,25 @@ namespace vg
             }
             return ok;
         };
-        // H1 = bf16(relu(D1 + b1)) into shared memory: this warp's rows and column slice
-        auto epilogue1 = [&]() {
+        // H1 = bf16(relu(D1 + b1)) into shared memory: this warp's rows and column slice.  Two
+        // columns per instruction: packed FP32 adds, and one conversion that rounds both sums to
+        // BF16 and clamps them at zero (ReLU commutes with round-to-nearest).
+        auto epilogue1 = [&](uint32_t acc) {
 #pragma unroll
             for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
             {
                 float v[32];
-                tc::tmem_load32(lane_base + static_cast<uint32_t>(c0), v);
+                tc::tmem_load32(lane_base + acc + static_cast<uint32_t>(c0), v);
 #pragma unroll
                 for (int j = 0; j < 32; j += 8)
                 {
-                    // two values per conversion instruction, each rounded to nearest as before
-                    __align__(16) __nv_bfloat162 h[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        h[k] = __floats2bfloat162_rn(fmaxf(__fadd_rn(v[j + 2 * k], sb1[c0 + j + 2 * k]), 0.0f),
-                                                     fmaxf(__fadd_rn(v[j + 2 * k + 1], sb1[c0 + j + 2 * k + 1]), 0.0f));
+                    const float4 ba = *reinterpret_cast<const float4 *>(sb1 + c0 + j);
+                    const float4 bb = *reinterpret_cast<const float4 *>(sb1 + c0 + j + 4);
+                    __align__(16) uint32_t h[4];
+                    h[0] = relu_bf16x2(__fadd2_rn(make_float2(v[j], v[j + 1]), make_float2(ba.x, ba.y)));
+                    h[1] = relu_bf16x2(__fadd2_rn(make_float2(v[j + 2], v[j + 3]), make_float2(ba.z, ba.w)));
+                    h[2] = relu_bf16x2(__fadd2_rn(make_float2(v[j + 4], v[j + 5]), make_float2(bb.x, bb.y)));
+                    h[3] = relu_bf16x2(__fadd2_rn(make_float2(v[j + 6], v[j + 7]), make_float2(bb.z, bb.w)));
                     *reinterpret_cast<uint4 *>(sh + tc::tile_offset(row, c0 + j, kHidden)) = *reinterpret_cast<const uint4 *>(h);
                 }
             }
@@ -907,24 +952,27 @@ namespace vg
             tc::fence_before_sync();
             __syncthreads();
         };
-        // z = bf16(relu(D2 + b2)) . w3 + b3: partial sums over this warp's 64 columns, added
-        // slice by slice in column order
-        auto epilogue2 = [&](long long tile) {
-            float z = 0.0f;
+        // z = bf16(relu(D2 + b2)) . w3 + b3: partial sums over this warp's 64 columns (even and
+        // odd columns in the two halves of packed FP32 multiply-adds), added slice by slice
+        auto epilogue2 = [&](long long tile, uint32_t acc) {
+            float2 z2 = make_float2(0.0f, 0.0f);
 #pragma unroll
             for (int c0 = c_lo; c0 < c_lo + 64; c0 += 32)
             {
                 float v[32];
-                tc::tmem_load32(lane_base + static_cast<uint32_t>(kHidden + c0), v);
+                tc::tmem_load32(lane_base + acc + static_cast<uint32_t>(c0), v);
 #pragma unroll
-                for (int j = 0; j < 32; j += 2)
+                for (int j = 0; j < 32; j += 4)
                 {
-                    const float2 h = __bfloat1622float2(__floats2bfloat162_rn(fmaxf(__fadd_rn(v[j], sb2[c0 + j]), 0.0f),
-                                                                              fmaxf(__fadd_rn(v[j + 1], sb2[c0 + j + 1]), 0.0f)));
-                    z = fmaf(h.x, sw3[c0 + j], z);
-                    z = fmaf(h.y, sw3[c0 + j + 1], z);
+                    const float4 bb = *reinterpret_cast<const float4 *>(sb2 + c0 + j);
+                    const float4 ww = *reinterpret_cast<const float4 *>(sw3 + c0 + j);
+                    const uint32_t h0 = relu_bf16x2(__fadd2_rn(make_float2(v[j], v[j + 1]), make_float2(bb.x, bb.y)));
+                    const uint32_t h1 = relu_bf16x2(__fadd2_rn(make_float2(v[j + 2], v[j + 3]), make_float2(bb.z, bb.w)));
+                    z2 = __ffma2_rn(bf16x2_to_float2(h0), make_float2(ww.x, ww.y), z2);
+                    z2 = __ffma2_rn(bf16x2_to_float2(h1), make_float2(ww.z, ww.w), z2);
                 }
             }
+            const float z = __fadd_rn(z2.x, z2.y);
             zpart[slice][row] = z;
             tc::fence_before_sync();
             __syncthreads();
@@ -942,41 +990,53 @@ namespace vg
         long long tile = blockIdx.x;
         if (tile < tiles)
         {
-            // prologue: layer 1 of the first tile, then its layer 2 in flight
-            features(tile);
+            // Layer 1 and layer 2 of a tile share one half of the 512 accumulator columns, the
+            // halves alternating from tile to tile: the next tile's layer 1, its epilogue and its
+            // layer 2 go into the other half while this tile's layer-2 result waits, so the next
+            // tile's layer 2 runs on the tensor core during this tile's layer-2 epilogue.
+            uint32_t acc = 0;
+            load_inputs();
+            features();
             tc::fence_smem_to_async();
             tc::fence_before_sync();
             __syncthreads();
-            issue_layer1();
+            issue_layer1(acc);
             ok = wait_for(&bar1, ph1, pend1);
             if (ok)
             {
-                epilogue1();
-                issue_layer2();
+                epilogue1(acc);
+                issue_layer2(acc);
             }
             while (ok)
             {
                 const long long next = tile + gridDim.x;
                 const bool has_next = next < tiles;
+                const uint32_t acc_next = acc ^ static_cast<uint32_t>(kHidden);
                 if (has_next)
-                    features(next);  // while this tile's layer 2 runs
+                {
+                    features();  // the next tile's, while this tile's layer 2 runs
+                }
                 tc::fence_smem_to_async();
                 tc::fence_before_sync();
                 __syncthreads();
-                ok = wait_for(&bar2, ph2, pend2);
+                ok = wait_for(&bar2, ph2, pend2);  // this tile's layer 2; H1 is free again
                 if (!ok)
                     break;
                 if (has_next)
-                    issue_layer1();  // runs while this tile's layer-2 epilogue reads columns 256-511
-                epilogue2(tile);
+                {
+                    // the other half was last read by the previous tile's layer-2 epilogue
+                    issue_layer1(acc_next);
+                    ok = wait_for(&bar1, ph1, pend1);
+                    if (!ok)
+                        break;
+                    epilogue1(acc_next);
+                    issue_layer2(acc_next);  // runs during this tile's layer-2 epilogue
+                }
+                epilogue2(tile, acc);
                 if (!has_next)
                     break;
-                ok = wait_for(&bar1, ph1, pend1);
-                if (!ok)
-                    break;
-                epilogue1();
-                issue_layer2();
                 tile = next;
+                acc = acc_next;
             }
         }
         if (!ok && tid == 0)
