@@ -403,6 +403,58 @@ def run_debug(args, world, rank, local):
                           "timing": "wall clock of the synchronous call (scratch allocation included)"}))
 
 
+def run_latency(args, world, rank, local):
+    """Latency of one validate_motion call (a planner's extension step) through the C ABI with
+    host buffers: 1,000 single edges of the 60-primitive scene, one call each (the block path:
+    all blocks of the edge checked at once), then batches of 8 and 64 edges per call, and the
+    same single edges as resident CUDA tensors through the edge kernels (verdict read back)."""
+    import torch
+
+    import vamp_gb300 as vg
+    from vamp_gb300 import scenes
+    from vamp_gb300._lib import check, lib
+    from vamp_gb300.api import _ptr
+
+    torch.cuda.set_device(local)
+    env = vg.Environment.from_scene(scenes.scene_config1(SCENE_SEED))
+    a, b = scenes.edges(vg.panda.s_m, vg.panda.s_a, 1000, 92)
+    out = np.zeros(64, np.uint8)
+    name = b"panda"
+
+    def host_call(lo, hi):
+        check(lib.vg_validate_motions(name, env.handle, _ptr(a[lo:hi]), _ptr(b[lo:hi]), hi - lo, 32, _ptr(out)))
+
+    for i in range(max(args.warmup, 3) * 10):
+        host_call(i, i + 1)
+    res = {}
+    for k in (1, 8, 64):
+        ts = []
+        for i in range(0, 1000 - k + 1, k):
+            t0 = time.perf_counter()
+            host_call(i, i + k)
+            ts.append(time.perf_counter() - t0)
+        res[k] = (1e6 * float(np.median(ts)), 1e6 * float(np.percentile(ts, 90)))
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    dout = torch.empty(1, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    hv = torch.empty(1, dtype=torch.uint8).pin_memory()
+    ts = []
+    for i in range(1000):
+        t0 = time.perf_counter()
+        check(lib.vg_validate_motions_device(name, env.handle, da[i:i + 1].data_ptr(), db[i:i + 1].data_ptr(), 1, 32,
+                                             dout.data_ptr(), None, stream))
+        hv.copy_(dout)
+        ts.append(time.perf_counter() - t0)
+    dev_us = 1e6 * float(np.median(ts))
+    if rank == 0:
+        print(json.dumps({"metric": "validate_motion latency on 1 GB300 (one call, host buffers)",
+                          "value": res[1][0], "unit": "us per call", "higher_is_better": False,
+                          "p90_us": res[1][1], "batch_8_us_per_call": res[8][0], "batch_64_us_per_call": res[64][0],
+                          "edge_kernel_resident_single_edge_us": dev_us,
+                          "reference_x86_us_per_edge_one_thread": 1e6 / REFERENCE_X86["edges_per_s_one_thread"],
+                          "calls": 1000, "workload": "panda, 60-primitive scene, resolution 32"}))
+
+
 def run_filter(args, world, rank, local):
     """Pointcloud filter (filter_pointcloud, collision/filter.hh:176-320) of 1,048,576 points on
     the surfaces of 30 random cuboids and cylinders plus 2% noise, with the reference's Panda
@@ -864,10 +916,12 @@ def main():
     ap.add_argument("--schedule", type=int, default=None,
                     help="GPU edge schedule (default: the autotuner's pick): 0 segment per edge, 1 warp per edge, "
                          "2 warp per edge with the register-rich build, 3 as 2 with free segments starting the next edge")
-    ap.add_argument("--workload", default="edges", choices=["edges", "capt", "mixed", "debug", "filter", "roadmap"],
+    ap.add_argument("--workload", default="edges",
+                    choices=["edges", "capt", "mixed", "debug", "filter", "roadmap", "latency"],
                     help="edges: the 65,536-edge primitive scene (default); capt: the pointcloud workload; "
                          "mixed: four robots in one CUDA graph; debug: per-sphere collision reports; "
-                         "filter: the pointcloud filter and CAPT build; roadmap: a batched PRM* roadmap")
+                         "filter: the pointcloud filter and CAPT build; roadmap: a batched PRM* roadmap; "
+                         "latency: single validate_motion calls through the C ABI")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
@@ -882,6 +936,8 @@ def main():
         run_filter(args, world, rank, local)
     elif args.workload == "roadmap":
         run_roadmap(args, world, rank, local)
+    elif args.workload == "latency":
+        run_latency(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

@@ -240,7 +240,11 @@ int vg_fkcc_blocks(const char *robot, vg_env *env, const float *q, size_t n_bloc
 
 /* ------------------------------------------------------------------------- checks (host)
  * Same as the device forms with host buffers: copies in, checks, copies out, and waits.
- * Pinned buffers (vg_host_alloc) make the copies fastest.  Staging memory is owned by env. */
+ * Pinned buffers (vg_host_alloc) make the copies fastest.  Staging memory is owned by env.
+ * vg_validate_motions and vg_validate_vectors check a batch of at most 4,096 blocks in all (a
+ * planner's single edge, say) block by block: the blocks are built on the host with the edge
+ * kernels' arithmetic and checked at once by the blocks kernel, an edge being valid when all its
+ * blocks are; larger batches go to the edge kernels.  The verdicts are the same either way. */
 int vg_validate_states(const char *robot, vg_env *env, const float *q, size_t n, uint8_t *out);
 int vg_validate_motions(
     const char *robot, vg_env *env, const float *a, const float *b, size_t n, int resolution, uint8_t *out);

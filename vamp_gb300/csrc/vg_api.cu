@@ -424,6 +424,129 @@ namespace vg
         return VG_OK;
     }
 
+    static int ensure_pinned(vg_env *e, size_t bytes)
+    {
+        if (bytes <= e->pin_cap)
+        {
+            return VG_OK;
+        }
+        if (e->h_pin)
+        {
+            cudaFreeHost(e->h_pin);
+            e->h_pin = nullptr;
+            e->pin_cap = 0;
+        }
+        VG_CUDA(cudaMallocHost(&e->h_pin, bytes), "cudaMallocHost(staging)");
+        e->pin_cap = bytes;
+        return VG_OK;
+    }
+
+    // Blocks of a host batch above which the batch goes to the edge kernels.
+    constexpr size_t kSmallBlocks = 4096;
+
+    // A small host batch of edges checked block by block.  Every block of every edge is built on
+    // the host with the edge kernels' arithmetic (the length summed in the x86 order and rounded
+    // once, n = max(ceil(length / W * resolution), 1), block 0 at fractions (k + 1) / W of the
+    // edge, block i = block 0 minus i steps of v / (W n), planning/validate.hh:24-56), the blocks
+    // go to the caller-given-blocks kernel in one launch, and an edge is valid when all of its
+    // blocks are: the verdicts of the edge kernels, which stop at the first colliding block.  All
+    // blocks of an edge run at once, where the edge kernels give one warp the whole edge, which
+    // is what the latency of a single edge (a planner's extension step) needs.  dist == nullptr:
+    // b holds goals (validate_motion), otherwise motion vectors and dist the lengths
+    // (validate_vector).  *handled = 0 when the batch has more than kSmallBlocks blocks.
+    static int small_motions(const RobotOps *r, vg_env *env, const float *a, const float *b, const float *dist, size_t n,
+                             int resolution, uint8_t *out, int *handled)
+    {
+        *handled = 0;
+        const int W = env->lanes, D = r->dim;
+        if (n > kSmallBlocks)
+            return VG_OK;
+        std::vector<int> nb(n);
+        size_t total = 0;
+        float v[32];
+        for (size_t e = 0; e < n; ++e)
+        {
+            float len;
+            if (dist)
+            {
+                len = dist[e];
+            }
+            else
+            {
+                // |b - a| as the edge kernels compute it (edge_length)
+                float sq[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                for (int d = 0; d < D; ++d)
+                {
+                    const float vd = b[e * D + d] - a[e * D + d];
+                    const float q2 = vd * vd;
+                    sq[d & 7] = d < 8 ? q2 : sq[d & 7] + q2;
+                }
+                const float a0 = sq[4] + sq[0], a1 = sq[5] + sq[1], a2 = sq[6] + sq[2], a3 = sq[7] + sq[3];
+                len = std::sqrt((a0 + a2) + (a1 + a3));
+            }
+            const float nf = std::ceil((len / static_cast<float>(W)) * static_cast<float>(resolution));
+            if (nf > static_cast<float>(kSmallBlocks))
+                return VG_OK;
+            nb[e] = static_cast<int>(nf > 1.0f ? nf : 1.0f);
+            total += static_cast<size_t>(nb[e]);
+            if (total > kSmallBlocks)
+                return VG_OK;
+        }
+        const size_t qb = total * W * D * sizeof(float);
+        const size_t qa = (qb + 255) & ~size_t(255);
+        if (int rc = ensure_pinned(env, qa + total))
+            return rc;
+        if (int rc = ensure_stage(env, qa + total))
+            return rc;
+        float *hq = static_cast<float *>(env->h_pin);
+        uint8_t *hv = static_cast<uint8_t *>(env->h_pin) + qa;
+        float q[8][32], bs[32];
+        size_t blk = 0;
+        for (size_t e = 0; e < n; ++e)
+        {
+            for (int d = 0; d < D; ++d)
+                v[d] = dist ? b[e * D + d] : b[e * D + d] - a[e * D + d];
+            const float denom = static_cast<float>(W * nb[e]);
+            for (int d = 0; d < D; ++d)
+                bs[d] = v[d] / denom;
+            for (int k = 0; k < W; ++k)
+            {
+                const float pct = static_cast<float>(k + 1) / static_cast<float>(W);
+                for (int d = 0; d < D; ++d)
+                    q[k][d] = std::fma(v[d], pct, a[e * D + d]);
+            }
+            for (int i = 0; i < nb[e]; ++i, ++blk)
+            {
+                for (int k = 0; k < W; ++k)
+                {
+                    for (int d = 0; d < D; ++d)
+                    {
+                        hq[(blk * W + k) * D + d] = q[k][d];
+                        q[k][d] = q[k][d] - bs[d];
+                    }
+                }
+            }
+        }
+        float *dq = static_cast<float *>(env->d_stage);
+        uint8_t *dv = static_cast<uint8_t *>(env->d_stage) + qa;
+        VG_CUDA(cudaMemcpyAsync(dq, hq, qb, cudaMemcpyHostToDevice, 0), "copy configuration blocks");
+        if (int rc = vg_fkcc_blocks_device(r->name, env, dq, total, dv, nullptr))
+            return rc;
+        VG_CUDA(cudaMemcpyAsync(hv, dv, total, cudaMemcpyDeviceToHost, 0), "copy block verdicts");
+        VG_CUDA(cudaStreamSynchronize(0), "synchronize");
+        blk = 0;
+        for (size_t e = 0; e < n; ++e)
+        {
+            uint8_t ok = 1;
+            for (int i = 0; i < nb[e]; ++i)
+                ok &= hv[blk + i];
+            out[e] = ok;
+            blk += static_cast<size_t>(nb[e]);
+        }
+        *handled = 1;
+        return VG_OK;
+    }
+
     void tuned_for(const vg_env *env, const RobotOps *r, int *schedule, int *blocks_per_sm)
     {
         *schedule = env->schedule >= 0 ? env->schedule : r->default_schedule;
@@ -600,6 +723,8 @@ void vg_env_destroy(vg_env *env)
         cudaFree(env->d_stage);
     if (env->d_order)
         cudaFree(env->d_order);
+    if (env->h_pin)
+        cudaFreeHost(env->h_pin);
     for (void *p : env->d_clouds)
         cudaFree(p);
     for (void *p : env->d_hf)
@@ -1195,6 +1320,15 @@ int vg_validate_motions(
         return set_error(VG_ERR_ARG, "vg_validate_motions: bad argument");
     if (n == 0)
         return VG_OK;
+    if (resolution < 1)
+        return set_error(VG_ERR_ARG, "vg_validate_motions: bad argument");
+    if (int rc = commit(env))
+        return rc;
+    int handled = 0;
+    if (int rc = small_motions(r, env, a, b, nullptr, n, resolution, out, &handled))
+        return rc;
+    if (handled)
+        return VG_OK;
     const size_t cb = ((n * r->dim * sizeof(float)) + 255) & ~size_t(255);
     if (int rc = ensure_stage(env, 2 * cb + n))
         return rc;
@@ -1218,6 +1352,15 @@ int vg_validate_vectors(const char *robot, vg_env *env, const float *start, cons
     if (!r || !env || (n && (!start || !vector || !distance || !out)))
         return set_error(VG_ERR_ARG, "vg_validate_vectors: bad argument");
     if (n == 0)
+        return VG_OK;
+    if (resolution < 1)
+        return set_error(VG_ERR_ARG, "vg_validate_vectors: bad argument");
+    if (int rc = commit(env))
+        return rc;
+    int handled = 0;
+    if (int rc = small_motions(r, env, start, vector, distance, n, resolution, out, &handled))
+        return rc;
+    if (handled)
         return VG_OK;
     const size_t cb = ((n * r->dim * sizeof(float)) + 255) & ~size_t(255);
     const size_t db_ = ((n * sizeof(float)) + 255) & ~size_t(255);

@@ -142,6 +142,9 @@ struct vg_env
     unsigned *d_counter = nullptr;
     void *d_stage = nullptr;
     size_t stage_cap = 0;
+    // pinned host staging of small host-pointer edge batches (their blocks, then their verdicts)
+    void *h_pin = nullptr;
+    size_t pin_cap = 0;
     // per-robot picks of vg_autotune_motions (cleared by vg_env_set_schedule)
     std::vector<vg::RobotTune> tuned;
     // incremented by every upload of the image: CUDA graphs that captured an older image (its
