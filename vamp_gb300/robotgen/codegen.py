@@ -405,6 +405,7 @@ TABLED = {"ur5", "fetch", "baxter"}
 SNAP32 = 1e-7
 # coarse environment queries evaluated together in one pass over the objects
 COARSE_BATCH = int(os.environ.get("VG_COARSE_BATCH", "4"))
+LOOPED_BATCH = int(os.environ.get("VG_LOOPED_BATCH", "2"))  # coarse spheres per query in the looped form
 
 
 def f32_down(v: float) -> float:
@@ -1015,30 +1016,31 @@ for (int c = 0; c < {len(model['self_checks'])}; ++c)
 }}""".split("\n")
     staged_body = head + ["float *const st = ctx.stage;"] + stage + coarse + env_section(True) + self_section(True)
     cut = next(i for i, l in enumerate(coarse) if l.startswith("unsigned ch["))
-    nb = -(-n_env // 4)
-    env_loops = f"""// coarse spheres of every environment-checked link, 4 at a time (one copy of the batched query)
+    lb = LOOPED_BATCH
+    nb = -(-n_env // lb)
+    env_loops = f"""// coarse spheres of every environment-checked link, {lb} at a time (one copy of the batched query)
 unsigned *const chs = ctx.wsc;
 #pragma unroll 1
 for (int b = 0; b < {nb}; ++b)
 {{
-    float4 sp[4];
+    float4 sp[{lb}];
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
+    for (int s = 0; s < {lb}; ++s)
     {{
-        const int k = 4 * b + s;
+        const int k = {lb} * b + s;
         // padding sphere: far away with radius -inf, it is never tested and never hits
         sp[s] = k < {n_env} ? make_float4(st[({c0} + 3 * k) * vg::kStageStride], st[({c0} + 3 * k + 1) * vg::kStageStride],
                                           st[({c0} + 3 * k + 2) * vg::kStageStride], {pre}CoarseR[k])
                             : make_float4(1.0e10f, 0.0f, 0.0f, -__int_as_float(0x7f800000));
     }}
-    unsigned h[4];
-    ctx.template env_many<4>(sp, ctx.alive, h);
+    unsigned h[{lb}];
+    ctx.template env_many<{lb}>(sp, ctx.alive, h);
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
+    for (int s = 0; s < {lb}; ++s)
     {{
-        if (4 * b + s < {n_env} && (threadIdx.x & 31) == 0)
+        if ({lb} * b + s < {n_env} && (threadIdx.x & 31) == 0)
         {{
-            chs[4 * b + s] = h[s];  // warp-uniform
+            chs[{lb} * b + s] = h[s];  // warp-uniform
         }}
     }}
 }}
