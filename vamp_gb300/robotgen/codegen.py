@@ -1052,7 +1052,7 @@ for (int k = 0; k < {n_env}; ++k)
     const unsigned need = chs[k] & ctx.alive;
     if (need)
     {{
-        const unsigned hit = env_fine<Ctx::kW, Ctx::kExt>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
+        const unsigned hit = env_fine_inline<Ctx::kW, Ctx::kExt>(ctx.env, st, {pre}EnvFrameS[k], {pre}EnvStart[k], {pre}EnvStart[k + 1], need);
         if (hit && !ctx.kill(hit)) return;
     }}
 }}""".split("\n")
@@ -1133,6 +1133,14 @@ for (int k = 0; k < {n_env}; ++k)
     // in `need`: the segments whose block collides.
     template <int W, bool kExt = false>
     static __device__ __noinline__ unsigned env_fine(const vg::EnvView &ev, const float *st, int f, int k0, int k1, unsigned need)
+    {{
+        return env_fine_inline<W, kExt>(ev, st, f, k0, k1, need);
+    }}
+
+    // The same, inlined into its caller (the looped environment section calls it from one place).
+    template <int W, bool kExt = false>
+    static __device__ __forceinline__ unsigned env_fine_inline(const vg::EnvView &ev, const float *st, int f, int k0, int k1,
+                                                               unsigned need)
     {{
         const vg::Frame fr = frame_at(st, f);
         unsigned dead = 0u;
