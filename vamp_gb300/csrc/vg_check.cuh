@@ -714,9 +714,11 @@ namespace vg
         // this warp's scratch (kWarpScratch words) for warp-uniform values such as per-link hit masks
         unsigned *wsc = nullptr;
 
+        // inlined at each call site: the table-driven robot forms call it from two places (coarse
+        // and fine spheres), and an out-of-line query costs them more than the second copy
         __device__ __forceinline__ unsigned env_hit(float x, float y, float z, float r, unsigned mask)
         {
-            return env_query<W, kExt>(env, x, y, z, r, mask);
+            return env_query_inline<W, kExt>(env, x, y, z, r, mask);
         }
 
         template <int NS>
