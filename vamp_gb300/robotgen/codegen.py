@@ -403,9 +403,11 @@ TABLED = {"ur5", "fetch", "baxter"}
 # FP32 constants this close to 0 or +-1 are folded to exact values: URDF angles such as
 # 1.570796325 leave ~1e-9 residues that only cost operations (their effect is below 1e-8 m)
 SNAP32 = 1e-7
-# coarse environment queries evaluated together in one pass over the objects
+# Coarse spheres queried together (one pass over the objects, up to the largest bound among
+# them): four in the unrolled environment section (one inlined copy per batch), two in the looped
+# one (one copy in all), the fastest of 1-11 measured on the Panda's 65,536-edge workload.
 COARSE_BATCH = int(os.environ.get("VG_COARSE_BATCH", "4"))
-LOOPED_BATCH = int(os.environ.get("VG_LOOPED_BATCH", "2"))  # coarse spheres per query in the looped form
+LOOPED_BATCH = int(os.environ.get("VG_LOOPED_BATCH", "2"))
 
 
 def f32_down(v: float) -> float:
